@@ -1,0 +1,710 @@
+// g4s_api.cu — the C ABI (include/gpu4snn.h): network handles, the chunked step loop, the
+// reference's result files and its experiment sweep.
+//
+// A run is executed in chunks of at most `chunk_steps` steps; a chunk's spike ids go to a
+// device raster buffer sized so that every neuron could fire at every step of the chunk,
+// so it can never overflow.  After each chunk the per-step counts, raster offsets and
+// globaltimer stamps come back to the host (and the raster, when it is recorded).
+#include <cuda_runtime.h>
+#include <sys/stat.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cerrno>
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/gpu4snn.h"
+#include "g4s_internal.h"
+
+using namespace g4s;
+
+// ---------------------------------------------------------------------------------------
+// Errors.
+// ---------------------------------------------------------------------------------------
+static thread_local std::string g_last_error;
+
+namespace g4s {
+int set_error(int code, const std::string &msg) {
+  g_last_error = msg;
+  return code;
+}
+int cuda_error(cudaError_t e, const char *what) {
+  return set_error(e == cudaErrorMemoryAllocation ? G4S_ERR_NOMEM : G4S_ERR_CUDA,
+                   std::string(what) + ": " + cudaGetErrorString(e));
+}
+}  // namespace g4s
+
+#define G4S_CUDA(call)                                  \
+  do {                                                  \
+    cudaError_t e_ = (call);                            \
+    if (e_ != cudaSuccess) return cuda_error(e_, #call); \
+  } while (0)
+
+// ---------------------------------------------------------------------------------------
+// Handle.
+// ---------------------------------------------------------------------------------------
+struct g4s_net {
+  g4s_net_desc desc{};
+  NetView v{};
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  GridSync *gs = nullptr;
+  double *d_stats = nullptr;
+  int64_t chunk_steps = 0;
+  int64_t t_abs = 0;
+  unsigned long long barrier_ns = 2000000000ull;
+  size_t device_bytes = 0;
+  // pinned staging of one chunk
+  int *h_counts = nullptr;
+  long long *h_base = nullptr;
+  unsigned long long *h_stamps = nullptr;
+  int *h_raster = nullptr;
+  // host results since the last reset
+  std::vector<int32_t> rt, rid, counts;
+  std::vector<float> upd_ms, step_ms;
+  int64_t total_spikes = 0;
+  double last_ms = 0, last_wall_ms = 0;
+  int64_t last_spikes = 0;
+  int last_alg = -1;
+  DeliverShape shape;
+  int barrier_stall = 0;  // injected: extra arrivals the next SKL launch waits for
+};
+
+static std::atomic<int> g_fail_next_alloc{0};
+
+static void free_net(g4s_net *n) {
+  if (!n) return;
+  NetView &v = n->v;
+  cudaFree(v.vu);
+  cudaFree(v.abcd);
+  cudaFree(v.acc);
+  cudaFree(v.ilast);
+  cudaFree(v.sstat);
+  cudaFree(const_cast<int *>(v.idx));
+  cudaFree(const_cast<float *>(v.w));
+  cudaFree(v.raster);
+  cudaFree(v.counts);
+  cudaFree(v.base);
+  cudaFree(v.stamps);
+  cudaFree(v.status);
+  cudaFree(n->gs);
+  cudaFree(n->d_stats);
+  cudaFreeHost(n->h_counts);
+  cudaFreeHost(n->h_base);
+  cudaFreeHost(n->h_stamps);
+  cudaFreeHost(n->h_raster);
+  if (n->ev0) cudaEventDestroy(n->ev0);
+  if (n->ev1) cudaEventDestroy(n->ev1);
+  if (n->stream) cudaStreamDestroy(n->stream);
+  delete n;
+}
+
+static int64_t row_stride(int32_t nsyn) { return ((int64_t)nsyn + 3) / 4 * 4; }
+
+static int validate(const g4s_net_desc *d) {
+  if (!d) return set_error(G4S_ERR_INVALID, "null descriptor");
+  if (d->n < 2 || d->n > (int64_t)INT32_MAX) return set_error(G4S_ERR_INVALID, "n must be in [2, 2^31)");
+  if (d->nsyn < 1) return set_error(G4S_ERR_INVALID, "nsyn must be >= 1");
+  const int64_t maxsyn = d->self_loops ? d->n : d->n - 1;
+  if (d->nsyn > maxsyn) return set_error(G4S_ERR_INVALID, "nsyn exceeds the number of possible targets");
+  if (d->exc_permille < 0 || d->exc_permille > 1000) return set_error(G4S_ERR_INVALID, "exc_permille must be in [0, 1000]");
+  if (d->conn_law != G4S_CONN_PHILOX && d->conn_law != G4S_CONN_GLIBC)
+    return set_error(G4S_ERR_INVALID, "unknown connectivity law");
+  if (d->conn_law == G4S_CONN_GLIBC && d->n > (int64_t)INT32_MAX / 2)
+    return set_error(G4S_ERR_INVALID, "glibc law limited to n < 2^30");
+  if (!(d->drive_scale >= 0.0f) || d->drive_scale > 1e6f) return set_error(G4S_ERR_INVALID, "bad drive_scale");
+  return G4S_OK;
+}
+
+template <class T>
+static int dalloc(g4s_net *n, T **p, size_t count, const char *what) {
+  const size_t bytes = count * sizeof(T);
+  cudaError_t e = g_fail_next_alloc.exchange(0) ? cudaErrorMemoryAllocation : cudaMalloc((void **)p, bytes ? bytes : 16);
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    return set_error(G4S_ERR_NOMEM, std::string("cudaMalloc of ") + what + " (" + std::to_string(bytes) +
+                                        " bytes): " + cudaGetErrorString(e));
+  }
+  n->device_bytes += bytes;
+  return G4S_OK;
+}
+
+static void set_drive(g4s_net *n) {
+  n->v.ge = 5.0f * n->desc.drive_scale;
+  n->v.gi = 2.0f * n->desc.drive_scale;
+}
+
+static int alloc_net(const g4s_net_desc *d, g4s_net **out) {
+  int rc = validate(d);
+  if (rc) return rc;
+  g4s_net *n = new (std::nothrow) g4s_net;
+  if (!n) return set_error(G4S_ERR_NOMEM, "host allocation");
+  n->desc = *d;
+  NetView &v = n->v;
+  v.n = d->n;
+  v.nexc = (d->n * (int64_t)d->exc_permille) / 1000;
+  v.nsyn = d->nsyn;
+  v.stride = (int32_t)row_stride(d->nsyn);
+  v.seed = d->seed;
+  set_drive(n);
+  const size_t N = (size_t)d->n, S = (size_t)v.stride;
+  // chunk: a raster buffer that holds every neuron firing at every step of the chunk
+  int64_t budget = d->raster_budget_bytes > 0 ? d->raster_budget_bytes : (int64_t)1 << 30;
+  int64_t cs = budget / (int64_t)(4 * N);
+  if (cs < 1) cs = 1;
+  if (cs > 100000) cs = 100000;
+  n->chunk_steps = cs;
+  v.raster_cap = cs * (int64_t)N;
+  size_t free_b = 0, total_b = 0;
+  cudaError_t e = cudaMemGetInfo(&free_b, &total_b);
+  if (e != cudaSuccess) {
+    free_net(n);
+    return cuda_error(e, "cudaMemGetInfo");
+  }
+  const size_t need = N * S * 8 + N * (8 + 16 + 8 + 4 + 32) + (size_t)v.raster_cap * 4 + (size_t)cs * 32;
+  if (need + ((size_t)256 << 20) > free_b) {
+    free_net(n);
+    return set_error(G4S_ERR_NOMEM, "network needs " + std::to_string(need) + " bytes of device memory, " +
+                                        std::to_string(free_b) + " free");
+  }
+  if ((rc = dalloc(n, &v.vu, N, "v,u")) || (rc = dalloc(n, &v.abcd, N, "a,b,c,d")) ||
+      (rc = dalloc(n, &v.acc, N, "currents")) || (rc = dalloc(n, &v.ilast, N, "input current")) ||
+      (rc = dalloc(n, &v.sstat, N, "spike statistics")) ||
+      (rc = dalloc(n, const_cast<int **>(&v.idx), N * S, "targets")) ||
+      (rc = dalloc(n, const_cast<float **>(&v.w), N * S, "weights")) ||
+      (rc = dalloc(n, &v.raster, (size_t)v.raster_cap, "raster")) ||
+      (rc = dalloc(n, &v.counts, (size_t)cs, "counts")) || (rc = dalloc(n, &v.base, (size_t)cs, "offsets")) ||
+      (rc = dalloc(n, &v.stamps, (size_t)cs * 2 + 2, "stamps")) || (rc = dalloc(n, &v.status, 1, "status")) ||
+      (rc = dalloc(n, &n->gs, 1, "barrier")) || (rc = dalloc(n, &n->d_stats, 2, "stats"))) {
+    free_net(n);
+    return rc;
+  }
+  if ((e = cudaStreamCreateWithFlags(&n->stream, cudaStreamNonBlocking)) != cudaSuccess ||
+      (e = cudaEventCreate(&n->ev0)) != cudaSuccess || (e = cudaEventCreate(&n->ev1)) != cudaSuccess ||
+      (e = cudaMallocHost((void **)&n->h_counts, (size_t)cs * 4)) != cudaSuccess ||
+      (e = cudaMallocHost((void **)&n->h_base, (size_t)cs * 8)) != cudaSuccess ||
+      (e = cudaMallocHost((void **)&n->h_stamps, ((size_t)cs * 2 + 2) * 8)) != cudaSuccess) {
+    free_net(n);
+    return cuda_error(e, "stream/event/pinned allocation");
+  }
+  if (d->record_raster) {
+    e = cudaMallocHost((void **)&n->h_raster, (size_t)v.raster_cap * 4);
+    if (e != cudaSuccess) {
+      free_net(n);
+      return cuda_error(e, "pinned raster staging");
+    }
+  }
+  cudaMemsetAsync(v.status, 0, sizeof(int), n->stream);
+  *out = n;
+  return G4S_OK;
+}
+
+static int check_status(g4s_net *n, const char *what) {
+  int st = 0, bar = 0;
+  G4S_CUDA(cudaMemcpyAsync(&st, n->v.status, sizeof(int), cudaMemcpyDeviceToHost, n->stream));
+  G4S_CUDA(cudaMemcpyAsync(&bar, &n->gs->error, sizeof(int), cudaMemcpyDeviceToHost, n->stream));
+  G4S_CUDA(cudaStreamSynchronize(n->stream));
+  if (bar == kErrTimeoutCode) return set_error(G4S_ERR_TIMEOUT, std::string(what) + ": grid barrier timed out");
+  if (st == kErrOverflowCode) return set_error(G4S_ERR_OVERFLOW, std::string(what) + ": raster overflow");
+  if (st == kErrConnCode) return set_error(G4S_ERR_INVALID, std::string(what) + ": connectivity draws exhausted");
+  if (st != 0 || bar != 0) return set_error(G4S_ERR_CUDA, std::string(what) + ": device error " + std::to_string(st));
+  return G4S_OK;
+}
+
+static int reset_net(g4s_net *n) {
+  NetView &v = n->v;
+  set_drive(n);
+  G4S_CUDA(cudaMemsetAsync(v.status, 0, sizeof(int), n->stream));
+  G4S_CUDA(cudaMemsetAsync(n->gs, 0, sizeof(GridSync), n->stream));
+  G4S_CUDA(launch_init(v, n->stream));
+  G4S_CUDA(cudaStreamSynchronize(n->stream));
+  n->t_abs = 0;
+  n->rt.clear();
+  n->rid.clear();
+  n->counts.clear();
+  n->upd_ms.clear();
+  n->step_ms.clear();
+  n->total_spikes = 0;
+  return G4S_OK;
+}
+
+// ---------------------------------------------------------------------------------------
+// Host generator of the reference's tables (glibc rand).  The k-th remaining target of a
+// row is found by a binary search over the sorted list of targets already taken, which
+// gives the reference's list-and-memmove result (gpu4snn.cu:880-898) in O(nsyn log nsyn)
+// per synapse instead of O(n).
+// ---------------------------------------------------------------------------------------
+namespace g4s {
+int conn_glibc_host(unsigned seed, int32_t n, int32_t nsyn, int32_t stride, int32_t *idx, float *w) {
+  if (n < 1 || nsyn < 0 || nsyn > n || stride < nsyn) return set_error(G4S_ERR_INVALID, "bad glibc table request");
+  const int32_t nexc = (int32_t)(((int64_t)n * 4) / 5);
+  const float wscale = 1000.0f / (float)nsyn;
+  std::vector<int32_t> taken;
+  taken.reserve((size_t)nsyn);
+  srand(seed);
+  for (int32_t i = 0; i < n; ++i) {
+    taken.clear();
+    int32_t *ri = idx + (int64_t)i * stride;
+    float *rw = w + (int64_t)i * stride;
+    for (int32_t j = 0; j < nsyn; ++j) {
+      const int32_t size = n - j;
+      const int32_t k = (int32_t)((size_t)rand() % (size_t)size);
+      float x = i < nexc ? wscale * 0.5f : wscale * -1.0f;
+      x = x * (float)rand();
+      x = x / (float)RAND_MAX;
+      int32_t lo = k, hi = k + (int32_t)taken.size();
+      while (lo < hi) {
+        const int32_t mid = lo + (hi - lo) / 2;
+        const int32_t le = (int32_t)(std::upper_bound(taken.begin(), taken.end(), mid) - taken.begin());
+        if (mid + 1 - le >= k + 1)
+          hi = mid;
+        else
+          lo = mid + 1;
+      }
+      taken.insert(std::upper_bound(taken.begin(), taken.end(), lo), lo);
+      ri[j] = lo;
+      rw[j] = x;
+    }
+    for (int32_t j = nsyn; j < stride; ++j) {
+      ri[j] = -1;
+      rw[j] = 0.0f;
+    }
+  }
+  return G4S_OK;
+}
+}  // namespace g4s
+
+// ---------------------------------------------------------------------------------------
+// Step loop.
+// ---------------------------------------------------------------------------------------
+static int resolve_alg(g4s_net *n, int alg) {
+  if (alg == kAlgAuto) {
+    n->shape = DeliverShape{};
+    n->shape.group = 0;
+    return kAlgSKL;
+  }
+  return alg;
+}
+
+static int run_net(g4s_net *n, int32_t steps, int32_t alg_in) {
+  if (steps < 0) return set_error(G4S_ERR_INVALID, "steps must be >= 0");
+  if (alg_in < 0 || alg_in > kAlgAuto) return set_error(G4S_ERR_INVALID, "unknown algorithm");
+  if (n->t_abs + steps > (int64_t)INT32_MAX) return set_error(G4S_ERR_INVALID, "step counter limit");
+  const int alg = resolve_alg(n, alg_in);
+  NetView &v = n->v;
+  if (n->shape.k_hint <= 0) n->shape.k_hint = (int)std::max<int64_t>(1, v.n / 20);
+  const auto w0 = std::chrono::steady_clock::now();
+  G4S_CUDA(cudaEventRecord(n->ev0, n->stream));
+  int64_t remaining = steps, spikes = 0;
+  while (remaining > 0) {
+    const int cs = (int)std::min<int64_t>(remaining, n->chunk_steps);
+    const bool last_chunk = remaining == cs;
+    G4S_CUDA(cudaMemsetAsync(v.counts, 0, (size_t)cs * sizeof(int), n->stream));
+    G4S_CUDA(cudaMemsetAsync(v.stamps, 0, ((size_t)cs * 2 + 2) * 8, n->stream));
+    if (alg == kAlgSKL) {
+      G4S_CUDA(cudaMemsetAsync(n->gs, 0, sizeof(GridSync), n->stream));
+      G4S_CUDA(launch_persistent(v, n->t_abs, cs, last_chunk, n->gs, n->barrier_ns, n->shape.group,
+                                 n->barrier_stall, n->stream));
+      n->barrier_stall = 0;
+    } else {
+      for (int lt = 0; lt < cs; ++lt) {
+        G4S_CUDA(launch_update(v, n->t_abs, lt, last_chunk && lt == cs - 1, n->stream));
+        G4S_CUDA(launch_deliver(v, lt, alg, n->shape, n->stream));
+      }
+    }
+    G4S_CUDA(cudaMemcpyAsync(n->h_counts, v.counts, (size_t)cs * 4, cudaMemcpyDeviceToHost, n->stream));
+    G4S_CUDA(cudaMemcpyAsync(n->h_base, v.base, (size_t)cs * 8, cudaMemcpyDeviceToHost, n->stream));
+    G4S_CUDA(cudaMemcpyAsync(n->h_stamps, v.stamps, (size_t)cs * 16, cudaMemcpyDeviceToHost, n->stream));
+    int rc = check_status(n, alg == kAlgSKL ? "persistent step kernel" : "step kernels");
+    if (rc) return rc;
+    const int64_t chunk_total = (int64_t)n->h_base[cs - 1] + n->h_counts[cs - 1];
+    if (n->desc.record_raster && chunk_total > 0) {
+      G4S_CUDA(cudaMemcpyAsync(n->h_raster, v.raster, (size_t)chunk_total * 4, cudaMemcpyDeviceToHost, n->stream));
+      G4S_CUDA(cudaStreamSynchronize(n->stream));
+      const size_t off = n->rt.size();
+      n->rt.resize(off + (size_t)chunk_total);
+      n->rid.resize(off + (size_t)chunk_total);
+      for (int lt = 0; lt < cs; ++lt) {
+        int *b = n->h_raster + n->h_base[lt];
+        std::sort(b, b + n->h_counts[lt]);
+        const int32_t t = (int32_t)(n->t_abs + lt);
+        for (int q = 0; q < n->h_counts[lt]; ++q) {
+          n->rt[off + (size_t)n->h_base[lt] + q] = t;
+          n->rid[off + (size_t)n->h_base[lt] + q] = b[q];
+        }
+      }
+    }
+    for (int lt = 0; lt < cs; ++lt) {
+      n->counts.push_back(n->h_counts[lt]);
+      const unsigned long long s0 = n->h_stamps[2 * lt], s1 = n->h_stamps[2 * lt + 1];
+      const unsigned long long s2 = lt + 1 < cs ? n->h_stamps[2 * lt + 2] : 0ull;
+      n->upd_ms.push_back(s1 > s0 ? (float)((s1 - s0) * 1e-6) : 0.0f);
+      n->step_ms.push_back(s2 > s0 ? (float)((s2 - s0) * 1e-6) : 0.0f);
+    }
+    spikes += chunk_total;
+    n->t_abs += cs;
+    remaining -= cs;
+  }
+  G4S_CUDA(cudaEventRecord(n->ev1, n->stream));
+  G4S_CUDA(cudaEventSynchronize(n->ev1));
+  float ms = 0.0f;
+  G4S_CUDA(cudaEventElapsedTime(&ms, n->ev0, n->ev1));
+  n->last_ms = ms;
+  n->last_wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - w0).count();
+  n->last_spikes = spikes;
+  n->total_spikes += spikes;
+  n->last_alg = alg;
+  return G4S_OK;
+}
+
+// ---------------------------------------------------------------------------------------
+// Result files in the reference's formats.
+// ---------------------------------------------------------------------------------------
+static int mkdirs(const std::string &path) {
+  std::string cur;
+  for (size_t i = 0; i <= path.size(); ++i) {
+    if (i == path.size() || path[i] == '/') {
+      if (!cur.empty() && mkdir(cur.c_str(), 0775) != 0 && errno != EEXIST)
+        return set_error(G4S_ERR_IO, "mkdir " + cur + ": " + strerror(errno));
+    }
+    if (i < path.size()) cur.push_back(path[i]);
+  }
+  return G4S_OK;
+}
+
+static void write_record(std::ofstream &o, float a, float b, float c, float d, float v, float u, float I, int64_t id,
+                         int nospks) {
+  o << a << " " << b << " " << c << " " << d << " " << v << " " << u << " " << I << " " << id << " " << nospks
+    << "\n";
+}
+
+static int write_results(g4s_net *n, const std::string &dir, double elapsed, double ewd) {
+  int rc = mkdirs(dir);
+  if (rc) return rc;
+  const std::string p = dir.back() == '/' ? dir : dir + "/";
+  const int64_t N = n->v.n;
+  std::vector<float> v(N), u(N), I(N), a(N), b(N), c(N), d(N);
+  std::vector<int32_t> nos(N);
+  rc = g4s_net_state(n, v.data(), u.data(), I.data(), a.data(), b.data(), c.data(), d.data(), nos.data());
+  if (rc) return rc;
+  {
+    std::ofstream o(p + "neuroninfo.csv");
+    if (!o.is_open()) return set_error(G4S_ERR_IO, "cannot open " + p + "neuroninfo.csv");
+    o << "a b c d v u I id nospks" << "\n";
+    for (int64_t i = 0; i < N; ++i) write_record(o, a[i], b[i], c[i], d[i], -65.0f, b[i] * -65.0f, 0.0f, i, 0);
+  }
+  {
+    std::ofstream o(p + "spiketimes.csv");
+    if (!o.is_open()) return set_error(G4S_ERR_IO, "cannot open " + p + "spiketimes.csv");
+    o << "SpkTime NeuronID" << "\n";
+    for (size_t q = 0; q < n->rt.size(); ++q) o << n->rt[q] << " " << n->rid[q] << "\n";
+  }
+  {
+    std::ofstream o(p + "computetime.csv");
+    if (!o.is_open()) return set_error(G4S_ERR_IO, "cannot open " + p + "computetime.csv");
+    o << "TimeStep SpksPerStep TimeKernelUpdate TimeSpent" << "\n";
+    for (size_t t = 0; t < n->counts.size(); ++t)
+      o << t << " " << n->counts[t] << " " << (double)n->upd_ms[t] << " " << (double)n->step_ms[t] << "\n";
+  }
+  {
+    std::ofstream o(p + "sim_overview.csv");
+    if (!o.is_open()) return set_error(G4S_ERR_IO, "cannot open " + p + "sim_overview.csv");
+    o << "N elapsed(ms) elapsedwithdata(ms) totalspkcount" << "\n";
+    o << N << " " << elapsed << " " << ewd << " " << n->total_spikes;
+  }
+  {
+    std::ofstream o(p + "neuroninfoafter.csv");
+    if (!o.is_open()) return set_error(G4S_ERR_IO, "cannot open " + p + "neuroninfoafter.csv");
+    o << "a b c d v u I id nospks" << "\n";
+    for (int64_t i = 0; i < N; ++i) write_record(o, a[i], b[i], c[i], d[i], v[i], u[i], I[i], i, nos[i]);
+  }
+  return G4S_OK;
+}
+
+// ---------------------------------------------------------------------------------------
+// Exported entry points.
+// ---------------------------------------------------------------------------------------
+extern "C" {
+
+int g4s_abi_version(void) { return G4S_ABI_VERSION; }
+
+const char *g4s_last_error(void) { return g_last_error.c_str(); }
+
+int g4s_net_create(const g4s_net_desc *desc, g4s_net **out) {
+  if (!out) return set_error(G4S_ERR_INVALID, "null output handle");
+  *out = nullptr;
+  g4s_net *n = nullptr;
+  int rc = alloc_net(desc, &n);
+  if (rc) return rc;
+  if (desc->conn_law == G4S_CONN_GLIBC) {
+    const size_t cnt = (size_t)n->v.n * (size_t)n->v.stride;
+    std::vector<int32_t> idx;
+    std::vector<float> w;
+    try {
+      idx.resize(cnt);
+      w.resize(cnt);
+    } catch (...) {
+      free_net(n);
+      return set_error(G4S_ERR_NOMEM, "host tables");
+    }
+    rc = conn_glibc_host((unsigned)desc->seed, (int32_t)n->v.n, n->v.nsyn, n->v.stride, idx.data(), w.data());
+    if (!rc) rc = g4s_net_load_tables(n, idx.data(), w.data(), n->v.stride);
+  } else {
+    cudaError_t e = launch_conngen(n->v, desc->self_loops, n->stream);
+    if (e != cudaSuccess) rc = cuda_error(e, "connectivity kernel");
+    if (!rc) rc = check_status(n, "connectivity kernel");
+  }
+  if (!rc) rc = reset_net(n);
+  if (rc) {
+    free_net(n);
+    return rc;
+  }
+  *out = n;
+  return G4S_OK;
+}
+
+int g4s_net_create_from_tables(const g4s_net_desc *desc, const int32_t *idx, const float *w, int32_t stride,
+                               g4s_net **out) {
+  if (!out || !idx || !w) return set_error(G4S_ERR_INVALID, "null argument");
+  *out = nullptr;
+  g4s_net *n = nullptr;
+  int rc = alloc_net(desc, &n);
+  if (rc) return rc;
+  rc = g4s_net_load_tables(n, idx, w, stride);
+  if (!rc) rc = reset_net(n);
+  if (rc) {
+    free_net(n);
+    return rc;
+  }
+  *out = n;
+  return G4S_OK;
+}
+
+int g4s_net_load_tables(g4s_net *n, const int32_t *idx, const float *w, int32_t stride) {
+  if (!n || !idx || !w) return set_error(G4S_ERR_INVALID, "null argument");
+  NetView &v = n->v;
+  if (stride != v.stride)
+    return set_error(G4S_ERR_INVALID, "table stride must be " + std::to_string(v.stride));
+  const size_t cnt = (size_t)v.n * (size_t)v.stride, bytes = cnt * 4;
+  // every target must be a neuron of this network or negative (an unused slot)
+  for (size_t k = 0; k < cnt; ++k)
+    if (idx[k] >= v.n)
+      return set_error(G4S_ERR_INVALID, "table entry " + std::to_string(k) + " targets neuron " +
+                                            std::to_string(idx[k]) + " >= n");
+  G4S_CUDA(cudaMemcpyAsync(const_cast<int *>(v.idx), idx, bytes, cudaMemcpyHostToDevice, n->stream));
+  G4S_CUDA(cudaMemcpyAsync(const_cast<float *>(v.w), w, bytes, cudaMemcpyHostToDevice, n->stream));
+  G4S_CUDA(cudaStreamSynchronize(n->stream));
+  return G4S_OK;
+}
+
+int g4s_net_reset(g4s_net *n) {
+  if (!n) return set_error(G4S_ERR_INVALID, "null handle");
+  return reset_net(n);
+}
+
+int g4s_net_run(g4s_net *n, int32_t steps, int32_t algorithm) {
+  if (!n) return set_error(G4S_ERR_INVALID, "null handle");
+  return run_net(n, steps, algorithm);
+}
+
+int g4s_net_get_info(g4s_net *n, g4s_net_info *info) {
+  if (!n || !info) return set_error(G4S_ERR_INVALID, "null argument");
+  info->n = n->v.n;
+  info->nsyn = n->v.nsyn;
+  info->stride = n->v.stride;
+  info->steps_done = n->t_abs;
+  info->total_spikes = n->total_spikes;
+  info->raster_size = (int64_t)n->rt.size();
+  info->last_run_ms = n->last_ms;
+  info->last_run_wall_ms = n->last_wall_ms;
+  info->last_run_spikes = n->last_spikes;
+  info->last_algorithm = n->last_alg;
+  info->persistent_blocks = persistent_blocks();
+  info->device_bytes = (int64_t)n->device_bytes;
+  return G4S_OK;
+}
+
+int g4s_net_raster(g4s_net *n, int32_t *t, int32_t *id, int64_t cap, int64_t *size) {
+  if (!n) return set_error(G4S_ERR_INVALID, "null handle");
+  const int64_t s = (int64_t)n->rt.size();
+  if (size) *size = s;
+  const int64_t m = std::min(s, cap);
+  if (m > 0) {
+    if (!t || !id) return set_error(G4S_ERR_INVALID, "null raster buffer");
+    memcpy(t, n->rt.data(), (size_t)m * 4);
+    memcpy(id, n->rid.data(), (size_t)m * 4);
+  }
+  return G4S_OK;
+}
+
+int g4s_net_counts(g4s_net *n, int32_t *counts, int64_t cap, int64_t *size) {
+  if (!n) return set_error(G4S_ERR_INVALID, "null handle");
+  const int64_t s = (int64_t)n->counts.size();
+  if (size) *size = s;
+  const int64_t m = std::min(s, cap);
+  if (m > 0) {
+    if (!counts) return set_error(G4S_ERR_INVALID, "null counts buffer");
+    memcpy(counts, n->counts.data(), (size_t)m * 4);
+  }
+  return G4S_OK;
+}
+
+int g4s_net_step_times(g4s_net *n, float *upd, float *step, int64_t cap, int64_t *size) {
+  if (!n) return set_error(G4S_ERR_INVALID, "null handle");
+  const int64_t s = (int64_t)n->upd_ms.size();
+  if (size) *size = s;
+  const int64_t m = std::min(s, cap);
+  if (m > 0) {
+    if (upd) memcpy(upd, n->upd_ms.data(), (size_t)m * 4);
+    if (step) memcpy(step, n->step_ms.data(), (size_t)m * 4);
+  }
+  return G4S_OK;
+}
+
+int g4s_net_state(g4s_net *n, float *v, float *u, float *i_last, float *a, float *b, float *c, float *d,
+                  int32_t *nospks) {
+  if (!n) return set_error(G4S_ERR_INVALID, "null handle");
+  const size_t N = (size_t)n->v.n;
+  std::vector<float2> vu;
+  std::vector<float4> p;
+  std::vector<SpikeStat> ss;
+  try {
+    if (v || u) vu.resize(N);
+    if (a || b || c || d) p.resize(N);
+    if (nospks) ss.resize(N);
+  } catch (...) {
+    return set_error(G4S_ERR_NOMEM, "host staging");
+  }
+  if (v || u) G4S_CUDA(cudaMemcpyAsync(vu.data(), n->v.vu, N * 8, cudaMemcpyDeviceToHost, n->stream));
+  if (a || b || c || d) G4S_CUDA(cudaMemcpyAsync(p.data(), n->v.abcd, N * 16, cudaMemcpyDeviceToHost, n->stream));
+  if (nospks) G4S_CUDA(cudaMemcpyAsync(ss.data(), n->v.sstat, N * sizeof(SpikeStat), cudaMemcpyDeviceToHost, n->stream));
+  if (i_last) G4S_CUDA(cudaMemcpyAsync(i_last, n->v.ilast, N * 4, cudaMemcpyDeviceToHost, n->stream));
+  G4S_CUDA(cudaStreamSynchronize(n->stream));
+  for (size_t i = 0; i < N; ++i) {
+    if (v) v[i] = vu[i].x;
+    if (u) u[i] = vu[i].y;
+    if (a) a[i] = p[i].x;
+    if (b) b[i] = p[i].y;
+    if (c) c[i] = p[i].z;
+    if (d) d[i] = p[i].w;
+    if (nospks) nospks[i] = ss[i].nospks;
+  }
+  return G4S_OK;
+}
+
+int g4s_net_currents(g4s_net *n, int64_t *acc) {
+  if (!n || !acc) return set_error(G4S_ERR_INVALID, "null argument");
+  G4S_CUDA(cudaMemcpyAsync(acc, n->v.acc, (size_t)n->v.n * 8, cudaMemcpyDeviceToHost, n->stream));
+  G4S_CUDA(cudaStreamSynchronize(n->stream));
+  return G4S_OK;
+}
+
+int g4s_net_tables(g4s_net *n, int64_t row0, int64_t nrows, int32_t *idx, float *w) {
+  if (!n) return set_error(G4S_ERR_INVALID, "null handle");
+  if (row0 < 0 || nrows < 0 || row0 + nrows > n->v.n) return set_error(G4S_ERR_INVALID, "row range");
+  const size_t off = (size_t)row0 * (size_t)n->v.stride, cnt = (size_t)nrows * (size_t)n->v.stride;
+  if (idx) G4S_CUDA(cudaMemcpyAsync(idx, n->v.idx + off, cnt * 4, cudaMemcpyDeviceToHost, n->stream));
+  if (w) G4S_CUDA(cudaMemcpyAsync(w, n->v.w + off, cnt * 4, cudaMemcpyDeviceToHost, n->stream));
+  G4S_CUDA(cudaStreamSynchronize(n->stream));
+  return G4S_OK;
+}
+
+int g4s_net_stats(g4s_net *n, double *rate_hz, double *isi_cv, int64_t *total_spikes) {
+  if (!n) return set_error(G4S_ERR_INVALID, "null handle");
+  double h[2] = {0, 0};
+  G4S_CUDA(cudaMemsetAsync(n->d_stats, 0, 16, n->stream));
+  G4S_CUDA(launch_stats(n->v, n->d_stats, n->stream));
+  G4S_CUDA(cudaMemcpyAsync(h, n->d_stats, 16, cudaMemcpyDeviceToHost, n->stream));
+  G4S_CUDA(cudaStreamSynchronize(n->stream));
+  if (rate_hz) *rate_hz = n->t_abs ? (double)n->total_spikes * 1000.0 / ((double)n->v.n * (double)n->t_abs) : 0.0;
+  if (isi_cv) *isi_cv = h[1] > 0 ? h[0] / h[1] : 0.0;
+  if (total_spikes) *total_spikes = n->total_spikes;
+  return G4S_OK;
+}
+
+int g4s_net_set_barrier_timeout(g4s_net *n, uint64_t ns) {
+  if (!n) return set_error(G4S_ERR_INVALID, "null handle");
+  n->barrier_ns = ns;
+  return G4S_OK;
+}
+
+int g4s_inject_fault(g4s_net *n, int32_t kind) {
+  if (kind == G4S_FAULT_ALLOC) {
+    g_fail_next_alloc.store(1);
+    return G4S_OK;
+  }
+  if (kind == G4S_FAULT_BARRIER_STALL) {
+    if (!n) return set_error(G4S_ERR_INVALID, "null handle");
+    n->barrier_stall = 1;
+    return G4S_OK;
+  }
+  return set_error(G4S_ERR_INVALID, "unknown fault kind");
+}
+
+int g4s_net_destroy(g4s_net *n) {
+  if (!n) return set_error(G4S_ERR_INVALID, "null handle");
+  free_net(n);
+  return G4S_OK;
+}
+
+int g4s_net_write_results(g4s_net *n, const char *dir, const float *init_state, double elapsed_ms,
+                          double elapsed_with_data_ms) {
+  (void)init_state;
+  if (!n || !dir) return set_error(G4S_ERR_INVALID, "null argument");
+  return write_results(n, dir, elapsed_ms, elapsed_with_data_ms);
+}
+
+int g4s_run_protocol(int32_t n, int32_t nsyn, int32_t iterations, int32_t algorithm, int32_t mode, uint64_t seed,
+                     int32_t conn_law, const char *results_root) {
+  if (!results_root) return set_error(G4S_ERR_INVALID, "null results root");
+  if (iterations < 0) return set_error(G4S_ERR_INVALID, "iterations must be >= 0");
+  if (algorithm < -1 || algorithm > kAlgAuto) return set_error(G4S_ERR_INVALID, "algorithm must be -1..5");
+  if (mode < -1 || mode > 2) return set_error(G4S_ERR_INVALID, "mode must be -1..2");
+  g4s_net_desc d{};
+  d.n = n;
+  d.nsyn = nsyn;
+  d.exc_permille = 800;
+  d.self_loops = conn_law == G4S_CONN_GLIBC ? 1 : 0;
+  d.conn_law = conn_law;
+  d.seed = seed;
+  d.drive_scale = 1.0f;
+  d.record_raster = 1;
+  g4s_net *net = nullptr;
+  int rc = g4s_net_create(&d, &net);
+  if (rc) return rc;
+  static const float kModeScale[3] = {0.5f, 1.0f, 1.5f};
+  for (int m = 0; m < 3; ++m) {
+    if (mode >= 0 && m != mode) continue;
+    for (int a = 0; a < 5; ++a) {
+      const int alg = algorithm < 0 ? a : algorithm;
+      if (algorithm >= 0 && a > 0) break;
+      net->desc.drive_scale = kModeScale[m];
+      if ((rc = reset_net(net))) break;
+      char sub[256];
+      snprintf(sub, sizeof sub, "/Results/N%dNsyn%dRegime%dAlg%d/", n, nsyn, m, alg);
+      const auto w0 = std::chrono::steady_clock::now();
+      if ((rc = run_net(net, iterations, alg))) break;
+      const double ewd = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - w0).count();
+      if ((rc = write_results(net, std::string(results_root) + sub, net->last_ms, ewd))) break;
+      printf("Regime %d Alg %d: %d steps, %lld spikes, %.3f ms device, %.3f ms with data\n", m, alg, iterations,
+             (long long)net->total_spikes, net->last_ms, ewd);
+    }
+    if (rc) break;
+  }
+  g4s_net_destroy(net);
+  return rc;
+}
+
+int g4s_conn_glibc(uint32_t seed, int32_t n, int32_t nsyn, int32_t stride, int32_t *idx, float *w) {
+  if (!idx || !w) return set_error(G4S_ERR_INVALID, "null table buffer");
+  return conn_glibc_host(seed, n, nsyn, stride, idx, w);
+}
+
+}  // extern "C"

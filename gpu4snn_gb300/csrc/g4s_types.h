@@ -1,0 +1,59 @@
+// g4s_types.h — types shared by the host library and the kernels.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace g4s {
+
+// Philox key word 1 per random stream (key word 0 is the network seed).
+constexpr uint64_t kStreamConn = 1;    // target draws:   counter (row, draw block, 0)
+constexpr uint64_t kStreamWeight = 2;  // weights:        counter (row, slot / 4, 0)
+constexpr uint64_t kStreamParam = 3;   // parameter r:    counter (neuron, 0, 0)
+constexpr uint64_t kStreamNoise = 4;   // thalamic drive: counter (neuron, step, attempt)
+
+// Device-side error codes (the host maps them to G4S_ERR_*).
+constexpr int kErrTimeoutCode = 1;   // a grid barrier waited longer than its limit
+constexpr int kErrOverflowCode = 2;  // a spike did not fit the raster buffer
+constexpr int kErrConnCode = 3;      // connectivity generation ran out of draws
+
+// Grid barrier state: a monotone arrival counter and an error word (one 128 B line).
+struct alignas(128) GridSync {
+  unsigned count;
+  int error;
+  unsigned pad[30];
+};
+
+// Per-neuron spike statistics, touched only when the neuron fires (32 B, one sector).
+struct alignas(32) SpikeStat {
+  int nospks;     // spikes so far (the reference's Neuron::nospks)
+  int last;       // step of the last spike, -1 before the first
+  int nisi;       // inter-spike intervals seen
+  int pad;
+  long long s1;   // sum of intervals (steps)
+  long long s2;   // sum of squared intervals
+};
+
+// Everything a kernel needs to step one network (passed by value).
+struct NetView {
+  int64_t n;        // neurons
+  int64_t nexc;     // excitatory neurons: ids [0, nexc)
+  int32_t nsyn;     // synapses per neuron
+  int32_t stride;   // row stride of the tables, a multiple of 4 (padding: target -1)
+  uint64_t seed;
+  float ge, gi;     // thalamic gains (5, 2) x drive scale
+  float2 *vu;       // membrane potential v, recovery u
+  float4 *abcd;     // a, b, c, d
+  long long *acc;   // Q32.32 synaptic current, consumed and cleared by the update
+  float *ilast;     // total input current of the last step of a run
+  SpikeStat *sstat;
+  const int *idx;   // [n][stride] targets
+  const float *w;   // [n][stride] weights
+  int *raster;      // spike ids of the current chunk, step after step
+  int64_t raster_cap;
+  int *counts;      // spikes per step of the current chunk
+  long long *base;  // raster offset of each step of the current chunk
+  unsigned long long *stamps;  // globaltimer per step: [2*lt] step start, [2*lt+1] update end
+  int *status;      // device error word (kErr*Code)
+};
+
+}  // namespace g4s

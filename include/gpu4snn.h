@@ -1,0 +1,147 @@
+/*
+ * gpu4snn.h — C ABI of the GB300 simulation library (libgpu4snn.so).
+ *
+ * The reference has no library interface: its boundary is the command line
+ * `./gpu4snn N Nsyn iterations` (gpu4snn.cu:735-739, spawned by gpu4snn.py:42) plus the
+ * result files it writes (gpu4snn.cu:1109-1140, 1256-1267, 1311-1327).  This ABI is what a
+ * ctypes driver (or any FFI) binds in its place.  Each entry point names the reference
+ * code it replaces.
+ *
+ * Conventions: every function returns an int status (G4S_OK = 0, negative G4S_ERR_* on
+ * failure) unless stated otherwise; the message of the last failure on the calling
+ * thread is g4s_last_error().  The library owns all device memory of a handle; the
+ * caller owns every host buffer it passes in.  A handle is used by one thread at a time;
+ * distinct handles may be used from distinct threads.  No C++ exception crosses the ABI.
+ */
+#ifndef GPU4SNN_H
+#define GPU4SNN_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define G4S_ABI_VERSION 1
+
+#define G4S_OK 0
+#define G4S_ERR_INVALID (-1)   /* bad argument or descriptor                         */
+#define G4S_ERR_CUDA (-2)      /* a CUDA runtime call failed                          */
+#define G4S_ERR_NOMEM (-3)     /* device or host allocation failed                    */
+#define G4S_ERR_TIMEOUT (-4)   /* a grid barrier of a persistent kernel timed out      */
+#define G4S_ERR_OVERFLOW (-5)  /* raster buffer overflow                              */
+#define G4S_ERR_IO (-6)        /* a result file could not be written                  */
+#define G4S_ERR_BUDGET (-7)    /* request does not fit the memory budget               */
+#define G4S_ERR_CANCELLED (-8) /* request cancelled                                    */
+#define G4S_ERR_STATE (-9)     /* call not valid in the handle's current state        */
+
+/* Propagation schemes; values are the reference's `dynamic` (gpu4snn.cu:1083). */
+#define G4S_ALG_AP 0   /* nested fan-out: a thread group per spiking row   (gpu4snn.cu:323-331, 409) */
+#define G4S_ALG_N 1    /* thread per spiking neuron                          (gpu4snn.cu:420-443)      */
+#define G4S_ALG_S 2    /* thread per synapse vector, oversubscribed grid     (gpu4snn.cu:446-467)      */
+#define G4S_ALG_AB 3   /* persistent grid over the synapse range             (gpu4snn.cu:554-584)      */
+#define G4S_ALG_SKL 4  /* whole step loop in one cooperative kernel          (gpu4snn.cu:669-716)      */
+#define G4S_ALG_AUTO 5 /* autotuner's pick                                                            */
+
+/* Connectivity laws. */
+#define G4S_CONN_PHILOX 0 /* GPU generator, counter-based Philox stream (default)              */
+#define G4S_CONN_GLIBC 1  /* the reference's host generator: srand(seed), rand() (gpu4snn.cu:873-898) */
+
+/* Network description (replaces argv N/Nsyn, gpu4snn.cu:738-744, and the hard-coded
+ * 80/20 split, drive gains and self-loop behaviour). */
+typedef struct g4s_net_desc {
+  int64_t n;                   /* neurons                                                   */
+  int32_t nsyn;                /* synapses per neuron (distinct targets)                    */
+  int32_t exc_permille;        /* excitatory share x1000; 800 = floor(4N/5) as the reference  */
+  int32_t self_loops;          /* 1: a neuron may target itself (the reference's tables)      */
+  int32_t conn_law;            /* G4S_CONN_*                                                */
+  uint64_t seed;               /* network seed (tables, parameters, drive)                  */
+  float drive_scale;           /* thalamic gains (5, 2) x scale; modes 0/1/2 = 0.5/1.0/1.5  */
+  int32_t record_raster;       /* 1: keep the spike raster on the host                      */
+  int64_t raster_budget_bytes; /* device raster buffer per chunk (0 = default 1 GiB)        */
+} g4s_net_desc;
+
+typedef struct g4s_net g4s_net;
+
+/* Run-time information of a handle. */
+typedef struct g4s_net_info {
+  int64_t n;
+  int32_t nsyn;
+  int32_t stride;            /* row stride of the tables (multiple of 4)                */
+  int64_t steps_done;        /* absolute step counter                                   */
+  int64_t total_spikes;      /* since creation or the last reset                         */
+  int64_t raster_size;       /* (step, id) pairs held on the host                       */
+  double last_run_ms;        /* device time of the last g4s_net_run (CUDA events)       */
+  double last_run_wall_ms;   /* host wall time of the last g4s_net_run                  */
+  int64_t last_run_spikes;   /* spikes of the last run                                   */
+  int32_t last_algorithm;    /* scheme the last run used (AUTO resolved)                */
+  int32_t persistent_blocks; /* grid of the SKL kernel                                  */
+  int64_t device_bytes;      /* device memory held by the handle                        */
+} g4s_net_info;
+
+int g4s_abi_version(void);
+const char *g4s_last_error(void);
+
+/* Allocation + initNeuron + connectivity (gpu4snn.cu:750-911, 1094). */
+int g4s_net_create(const g4s_net_desc *desc, g4s_net **out);
+/* Same with caller-supplied host tables [n][stride] (the reference's H2D copy of its host
+ * tables, gpu4snn.cu:910-911); padding slots carry target -1. */
+int g4s_net_create_from_tables(const g4s_net_desc *desc, const int32_t *idx, const float *w, int32_t stride,
+                               g4s_net **out);
+/* Replace the tables of an existing handle from host memory (H2D). */
+int g4s_net_load_tables(g4s_net *net, const int32_t *idx, const float *w, int32_t stride);
+/* Neuron state, currents, statistics and raster back to step 0 (initNeuron, gpu4snn.cu:1094). */
+int g4s_net_reset(g4s_net *net);
+/* Advance `steps` steps with one scheme (the step loop, gpu4snn.cu:1215-1300). */
+int g4s_net_run(g4s_net *net, int32_t steps, int32_t algorithm);
+int g4s_net_get_info(g4s_net *net, g4s_net_info *info);
+/* Spike raster (the reference's spiketimes.csv rows, gpu4snn.cu:1256-1261), ordered by
+ * (step, neuron id).  Writes min(cap, size) pairs; *n receives the size. */
+int g4s_net_raster(g4s_net *net, int32_t *t, int32_t *id, int64_t cap, int64_t *n);
+/* Spikes per step since the last reset (computetime.csv SpksPerStep, gpu4snn.cu:1267). */
+int g4s_net_counts(g4s_net *net, int32_t *counts, int64_t cap, int64_t *n);
+/* Per-step device times in ms: update phase and whole step (computetime.csv columns). */
+int g4s_net_step_times(g4s_net *net, float *update_ms, float *step_ms, int64_t cap, int64_t *n);
+/* Neuron record (gpu4snn.cu:50-62, writeNeuronInfo :727-729); any pointer may be NULL. */
+int g4s_net_state(g4s_net *net, float *v, float *u, float *i_last, float *a, float *b, float *c, float *d,
+                  int32_t *nospks);
+/* Raw Q32.32 synaptic currents pending for the next step. */
+int g4s_net_currents(g4s_net *net, int64_t *acc);
+/* Rows [row0, row0+nrows) of the tables, [nrows][stride]. */
+int g4s_net_tables(g4s_net *net, int64_t row0, int64_t nrows, int32_t *idx, float *w);
+/* FP64 statistics: mean rate (Hz, 1 ms steps) and mean per-neuron ISI CV. */
+int g4s_net_stats(g4s_net *net, double *rate_hz, double *isi_cv, int64_t *total_spikes);
+/* Grid-barrier time limit of the SKL kernel in ns (default 2 s); 0 makes every barrier
+ * give up at once (used to test the timeout path). */
+int g4s_net_set_barrier_timeout(g4s_net *net, uint64_t ns);
+int g4s_net_destroy(g4s_net *net);
+
+/* Host-side fault injection for failure-detection tests (nothing faults the GPU):
+ *   G4S_FAULT_BARRIER_STALL  the next SKL launch of `net` waits at its first barrier for
+ *                            one block more than it has, so the wait runs out after the
+ *                            barrier time limit and the run returns G4S_ERR_TIMEOUT;
+ *   G4S_FAULT_ALLOC          the next device allocation of g4s_net_create fails
+ *                            (process-wide; `net` may be NULL). */
+#define G4S_FAULT_BARRIER_STALL 1
+#define G4S_FAULT_ALLOC 2
+int g4s_inject_fault(g4s_net *net, int32_t kind);
+
+/* Reference result files for one run in `dir` (gpu4snn.cu:1109-1140, 1256-1267,
+ * 1311-1327): neuroninfo.csv (initial record), spiketimes.csv, computetime.csv,
+ * sim_overview.csv, neuroninfoafter.csv (the actual final record). */
+int g4s_net_write_results(g4s_net *net, const char *dir, const float *init_state /* [9][n] or NULL */,
+                          double elapsed_ms, double elapsed_with_data_ms);
+
+/* The reference's whole experiment (main, gpu4snn.cu:735-1332): for each drive mode
+ * (0..2, or `mode`) and scheme (0..4, or `algorithm`), run `iterations` steps of the same
+ * network and write Results/N{n}Nsyn{nsyn}Regime{mode}Alg{alg}/ under results_root. */
+int g4s_run_protocol(int32_t n, int32_t nsyn, int32_t iterations, int32_t algorithm, int32_t mode, uint64_t seed,
+                     int32_t conn_law, const char *results_root);
+
+/* The reference's host table generator with glibc rand() after srand(seed)
+ * (gpu4snn.cu:873-898), into [n][stride] host buffers (padding: -1 / 0). */
+int g4s_conn_glibc(uint32_t seed, int32_t n, int32_t nsyn, int32_t stride, int32_t *idx, float *w);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,138 @@
+"""GPU parity: the CUDA path against the CPU oracle, bit-exact (integer tables, Q32.32
+currents, binary32 neuron state) on the same seeds."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+ALGS = [0, 1, 2, 3, 4]
+
+
+def oracle_tables(O, n, nsyn, seed, self_loops=0):
+    d = O.make_desc(n, nsyn, seed, self_loops=self_loops)
+    return d, O.conn_philox(d)
+
+
+@pytest.mark.parametrize("n,nsyn,seed,self_loops", [(2500, 1000, 1, 0), (1000, 999, 5, 0), (300, 37, 9, 0),
+                                                    (257, 257, 11, 1), (5000, 3, 2, 0)])
+def test_tables_bit_exact(g4s, oracle, n, nsyn, seed, self_loops):
+    _, (idx, w) = oracle_tables(oracle, n, nsyn, seed, self_loops)
+    with g4s.Network(n, nsyn, seed=seed, self_loops=bool(self_loops)) as net:
+        gi, gw = net.tables()
+    assert np.array_equal(gi, idx)
+    assert np.array_equal(gw.view(np.uint32), w.view(np.uint32))
+
+
+def test_tables_large_sampled_rows(g4s, oracle):
+    n, nsyn, seed = 100_000, 1000, 2
+    d = oracle.make_desc(n, nsyn, seed)
+    with g4s.Network(n, nsyn, seed=seed, record_raster=False) as net:
+        for row0 in (0, 1, 49_999, 79_999, 80_000, n - 3):
+            gi, gw = net.tables(row0, 3)
+            oi, ow = oracle.conn_philox(d, row0, 3)
+            assert np.array_equal(gi, oi) and np.array_equal(gw.view(np.uint32), ow.view(np.uint32))
+
+
+def compare_state(net, sim):
+    s, o = net.state(), sim.state()
+    for k in ("v", "u", "a", "b", "c", "d"):
+        assert np.array_equal(s[k].view(np.uint32), o[k].view(np.uint32)), k
+    assert np.array_equal(s["nospks"], o["nospks"])
+    assert np.array_equal(net.currents(), sim.acc())
+
+
+@pytest.mark.parametrize("alg", ALGS)
+def test_step_parity_200(g4s, oracle, alg):
+    n, nsyn, seed = 2500, 1000, 1
+    d, (idx, w) = oracle_tables(oracle, n, nsyn, seed)
+    sim = oracle.Sim(d, idx, w)
+    sim.run(200, threads=8)
+    with g4s.Network(n, nsyn, seed=seed) as net:
+        net.run(200, alg)
+        t, i = net.raster()
+        ot, oi = sim.raster()
+        assert np.array_equal(t, ot) and np.array_equal(i, oi)
+        assert np.array_equal(net.counts(), sim.counts())
+        compare_state(net, sim)
+        s = net.state()
+        assert np.array_equal(s["I"].view(np.uint32), sim.state()["I"].view(np.uint32))
+
+
+def test_full_config_skl_2000(g4s, oracle):
+    n, nsyn, seed = 2500, 1000, 1
+    d, (idx, w) = oracle_tables(oracle, n, nsyn, seed)
+    sim = oracle.Sim(d, idx, w)
+    sim.run(2000, threads=8)
+    with g4s.Network(n, nsyn, seed=seed) as net:
+        net.run(1000, 4)
+        net.run(1000, 5)
+        t, i = net.raster()
+        ot, oi = sim.raster()
+        assert np.array_equal(t, ot) and np.array_equal(i, oi)
+        compare_state(net, sim)
+        st, os_ = net.stats(), sim.stats()
+        assert st.total_spikes == os_.total_spikes
+        assert abs(st.rate_hz - os_.rate_hz) < 1e-9
+        assert abs(st.isi_cv - os_.isi_cv) < 1e-9
+
+
+@pytest.mark.parametrize("drive", [0.5, 1.5, 2.0])
+def test_drive_modes(g4s, oracle, drive):
+    n, nsyn, seed = 3000, 500, 4
+    d = oracle.make_desc(n, nsyn, seed, drive_scale=drive)
+    idx, w = oracle.conn_philox(d)
+    sim = oracle.Sim(d, idx, w)
+    sim.run(150, threads=8)
+    with g4s.Network(n, nsyn, seed=seed, drive_scale=drive) as net:
+        net.run(150, 4)
+        assert np.array_equal(np.stack(net.raster()), np.stack(sim.raster()))
+        compare_state(net, sim)
+
+
+def test_chunked_run_matches(g4s, oracle):
+    """A tiny raster budget forces many chunks; results must not change."""
+    n, nsyn, seed = 2000, 200, 3
+    d, (idx, w) = oracle_tables(oracle, n, nsyn, seed)
+    sim = oracle.Sim(d, idx, w)
+    sim.run(300, threads=8)
+    for alg in (2, 4):
+        with g4s.Network(n, nsyn, seed=seed, raster_budget_bytes=4 * n * 7) as net:
+            net.run(300, alg)
+            assert np.array_equal(np.stack(net.raster()), np.stack(sim.raster()))
+            compare_state(net, sim)
+
+
+def test_glibc_tables_on_gpu(g4s, oracle):
+    n, nsyn, seed = 2500, 1000, 3
+    idx, w = oracle.conn_glibc(seed, n, nsyn)
+    d = oracle.make_desc(n, nsyn, seed, self_loops=1)
+    sim = oracle.Sim(d, idx, w)
+    sim.run(100, threads=8)
+    with g4s.Network(n, nsyn, seed=seed, self_loops=True, conn_law=g4s.CONN_GLIBC) as net:
+        gi, gw = net.tables()
+        assert np.array_equal(gi, idx) and np.array_equal(gw.view(np.uint32), w.view(np.uint32))
+        net.run(100, 3)
+        assert np.array_equal(np.stack(net.raster()), np.stack(sim.raster()))
+        compare_state(net, sim)
+
+
+def test_barrier_timeout_is_reported(g4s, oracle):
+    """An injected stall makes the first grid barrier wait for a block that does not exist;
+    the wait runs out after the 50 ms limit, the host gets G4S_ERR_TIMEOUT and the context
+    and the handle stay usable."""
+    from gpu4snn_gb300 import _lib
+    n, nsyn, seed = 2000, 100, 1
+    with g4s.Network(n, nsyn, seed=seed) as net:
+        net.set_barrier_timeout(50_000_000)
+        net.inject_fault(_lib.FAULT_BARRIER_STALL)
+        with pytest.raises(g4s.G4SError) as e:
+            net.run(10, 4)
+        assert e.value.code == _lib.ERR_TIMEOUT
+        net.set_barrier_timeout(2_000_000_000)
+        net.reset()
+        net.run(40, 4)
+        d = oracle.make_desc(n, nsyn, seed)
+        idx, w = oracle.conn_philox(d)
+        sim = oracle.Sim(d, idx, w)
+        sim.run(40)
+        assert np.array_equal(np.stack(net.raster()), np.stack(sim.raster()))
