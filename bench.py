@@ -1,0 +1,324 @@
+"""Benchmark of the GPU4SNN simulation step on GB300 (one JSON line on stdout).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload NAME]
+
+Workload (default "n100k"): one randomly connected Izhikevich network, N=100,000 neurons,
+Nsyn=1000 distinct targets each (1e8 synapses, int32 target + fp32 weight = 0.8 GB), the
+balanced drive (gains 5 and 2), seed 2.  One bench step is one 10,000-step simulation
+(10 s of model time).  The tables (0.8 GB) are larger than L2 (129 MB) and are streamed
+from HBM every step, so no L2 flush is needed between bench steps.
+
+Metric: synaptic events/s = sum over steps of spikes x Nsyn, divided by the device time of
+the runs (CUDA events on the library's launching stream).  `roofline` reports the
+persistent step kernel against the measured HBM copy bandwidth; `e2e` is the same metric
+through the C ABI with host tables uploaded from pinned memory, a reset, the run and the
+raster read back, every step.  `cpu_baseline` is the oracle's OpenMP port on the host cores.
+
+--impl reference times the reference's algorithm on the CPU (the oracle's OpenMP port of
+gpu4snn.cu's step, all host threads) on the same network; the reference itself has no CPU
+implementation of the step and its CUDA program cannot be built on the GPU host (its
+sources are not shipped there).
+
+Multi-GPU: the path does not shard; `--gpus N` under torchrun runs N independent replicas
+(seed + rank), value = all ranks' events / the slowest rank's time ("scaling": "weak").
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    # name: (N, Nsyn, sim steps per bench step, drive scale, seed)
+    "n100k": (100_000, 1000, 10_000, 1.0, 2),
+    "n1m": (1_000_000, 1000, 1000, 1.0, 3),
+    "n250k_s10k": (250_000, 10_000, 500, 1.0, 4),
+    "n2500": (2500, 1000, 2000, 1.0, 1),
+    "n25k": (25_000, 1000, 500, 1.0, 5),  # small profiling case: 0.2 GB of tables, still > L2
+}
+# algorithmic bytes: delivery = spikes x Nsyn x (4 B target + 4 B weight); update per
+# neuron and step = v,u read+write (16) + a,b,c,d (16) + current read (8)
+UPDATE_BYTES_PER_NEURON = 40
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.path = tempfile.mktemp(prefix="g4s_clocks_", suffix=".csv")
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if not self.proc or not os.path.exists(self.path):
+            return None
+        sm, smax, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = max(smax, float(parts[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        pg = dist
+    return ws, rank, local, pg
+
+
+def reduce_max(pg, x: float) -> float:
+    if pg is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def reduce_sum(pg, x: float) -> float:
+    if pg is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.SUM)
+    return float(t.item())
+
+
+def cpu_port_rate(n, nsyn, seed, drive, threads, min_seconds, max_steps, warm_steps):
+    """Events/s of the oracle's OpenMP port on a bounded sample of the workload."""
+    from oracle import g4s_oracle as O
+    d = O.make_desc(n, nsyn, seed, drive_scale=drive)
+    idx, w = O.conn_philox(d)
+    sim = O.Sim(d, idx, w)
+    sim.run(warm_steps, threads=threads)
+    spikes0, steps, t0 = len(sim.raster()[0]), 0, time.perf_counter()
+    while steps < max_steps and time.perf_counter() - t0 < min_seconds:
+        sim.run(25, threads=threads)
+        steps += 25
+    dt = time.perf_counter() - t0
+    ev = (len(sim.raster()[0]) - spikes0) * nsyn
+    return ev / dt, steps, dt
+
+
+def run_reference(a, cfg, ws, rank, pg):
+    if rank != 0:
+        return 0
+    n, nsyn, T, drive, seed = cfg
+    threads = os.cpu_count() or 1
+    from oracle import g4s_oracle as O
+    O.build()
+    d = O.make_desc(n, nsyn, seed, drive_scale=drive)
+    idx, w = O.conn_philox(d)
+    sim = O.Sim(d, idx, w)
+    per = max(1, min(T, 100))
+    for _ in range(a.warmup):
+        sim.run(per, threads=threads)
+    s0 = len(sim.raster()[0])
+    t0 = time.perf_counter()
+    for _ in range(a.steps):
+        sim.run(per, threads=threads)
+    dt = time.perf_counter() - t0
+    ev = (len(sim.raster()[0]) - s0) * nsyn
+    v = ev / dt
+    sample = (f"{a.steps} x {per} simulation steps (after {a.warmup} x {per} warm-up) of the N={n}, Nsyn={nsyn} "
+              f"network, oracle OpenMP port, {threads} threads")
+    line = {"impl": "reference", "metric": "synaptic events/s", "value": v, "unit": "events/s", "n_gpus": ws,
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": dt * 1e3 / a.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+i64", "data": "synthetic (seeded Philox network)",
+            "config": workload_config(a.workload, cfg),
+            "cpu_baseline": {"value": v, "unit": "events/s", "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": "events/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def workload_config(name, cfg):
+    n, nsyn, T, drive, seed = cfg
+    return {"workload": name, "N": n, "Nsyn": nsyn, "sim_steps_per_bench_step": T, "drive_scale": drive,
+            "seed": seed, "synapses": n * nsyn, "table_bytes": n * ((nsyn + 3) // 4 * 4) * 8,
+            "l2": "tables larger than L2 (129 MB), streamed from HBM every step; no flush",
+            "parallelism": "replicas"}
+
+
+def load_traffic(name):
+    p = os.path.join(ROOT, "profiles", "persistent_step_traffic.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get(name)
+    return None
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="n100k")
+    ap.add_argument("--algorithm", default="AUTO")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
+    ap.add_argument("--raster-budget-mb", type=int, default=0, help="device raster buffer per chunk (0: default)")
+    a = ap.parse_args()
+    if a.warmup < 3:
+        a.warmup = 3
+    ws, rank, local, pg = dist_setup()
+    cfg = WORKLOADS[a.workload]
+    if a.impl == "reference":
+        return run_reference(a, cfg, ws, rank, pg)
+
+    import gpu4snn_gb300 as g
+    from gpu4snn_gb300 import _lib
+    n, nsyn, T, drive, seed = cfg
+    seed = seed + rank
+    _lib.check(g.load().g4s_set_device(local))
+    alg = g.ALG_NAMES[a.algorithm.upper()] if not a.algorithm.isdigit() else int(a.algorithm)
+    budget = a.raster_budget_mb << 20
+    net = g.Network(n, nsyn, seed=seed, drive_scale=drive, record_raster=False, raster_budget_bytes=budget)
+    for _ in range(a.warmup):
+        net.run(T, alg)
+    runs = []
+    if pg:
+        pg.barrier()
+    with ClockSampler(local) as clk:
+        w0 = time.perf_counter()
+        for _ in range(a.steps):
+            net.run(T, alg)
+            inf = net.info()
+            u, s = net.step_times()
+            runs.append((inf.last_run_ms, inf.last_run_kernel_ms, inf.last_run_spikes, inf.last_run_launches,
+                         float(u[-T:].sum()), float(s[-T:].sum()), inf.last_algorithm))
+        wall = time.perf_counter() - w0
+    if pg:
+        pg.barrier()
+    clocks = clk.summary()
+    dev_ms = sum(r[0] for r in runs)
+    kern_ms = sum(r[1] for r in runs)
+    spikes = sum(r[2] for r in runs)
+    launches = sum(r[3] for r in runs)
+    events = spikes * nsyn
+    t_max = reduce_max(pg, dev_ms)
+    ev_all = reduce_sum(pg, float(events))
+    value = ev_all / (t_max * 1e-3)
+    peak, peak_kind = peaks()
+    deliv_bytes = events * 8
+    upd_bytes = n * T * a.steps * UPDATE_BYTES_PER_NEURON
+    n_launch = max(1, launches)
+    achieved = (deliv_bytes + upd_bytes) / n_launch / (kern_ms / n_launch * 1e-3) / 1e9
+    upd_ms = sum(r[4] for r in runs)
+    deliv_ms = max(1e-9, sum(r[5] for r in runs) - upd_ms)
+    roofline = {"kernel": "k_persistent (SKL: fused update + delivery, all steps of a chunk)", "bound": "hbm",
+                "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "peak_source": f"{peak_kind} hbm_gbs", "traffic": load_traffic(a.workload),
+                "algorithmic_bytes_per_launch": (deliv_bytes + upd_bytes) / n_launch,
+                "launch_ms": kern_ms / n_launch,
+                "delivery_phase": {"bytes": deliv_bytes, "ms": deliv_ms, "gbs": deliv_bytes / deliv_ms / 1e6,
+                                   "frac": deliv_bytes / deliv_ms / 1e6 / peak},
+                "update_phase": {"bytes": upd_bytes, "ms": upd_ms, "gbs": upd_bytes / max(upd_ms, 1e-9) / 1e6}}
+    line = {"metric": "synaptic events/s", "value": value, "unit": "events/s", "n_gpus": ws, "steps": a.steps,
+            "warmup": a.warmup, "ms_per_step": t_max / a.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32+i64", "data": "synthetic (seeded Philox network)",
+            "config": workload_config(a.workload, cfg), "algorithm": int(runs[-1][6]),
+            "firing_rate_hz": spikes / (n * T * a.steps) * 1000.0, "wall_s": wall,
+            "roofline": roofline, "clocks": clocks, "gpu_launches": int(launches)}
+    # end to end through the C ABI with host buffers
+    if not a.no_e2e:
+        idx_h, p_idx = _lib.pinned_empty((n, net.stride), "int32")
+        w_h, p_w = _lib.pinned_empty((n, net.stride), "float32")
+        idx_h[:], w_h[:] = net.tables()
+        net.close()
+        e2e_net = g.Network(n, nsyn, seed=seed, drive_scale=drive, record_raster=True)
+        e2e_net.load_tables(idx_h, w_h)
+        e2e_net.reset()
+        e2e_net.run(T, alg)
+        e_ev, e_wall, d2h = 0, 0.0, 0
+        for _ in range(max(1, min(a.steps, 3))):
+            t0 = time.perf_counter()
+            e2e_net.load_tables(idx_h, w_h)
+            e2e_net.reset()
+            e2e_net.run(T, alg)
+            rt, rid = e2e_net.raster()
+            cnt = e2e_net.counts()
+            e_wall += time.perf_counter() - t0
+            e_ev += len(rt) * nsyn
+            d2h = len(rt) * 4 + T * (4 + 8 + 16)
+        k = max(1, min(a.steps, 3))
+        e_wall = reduce_max(pg, e_wall)
+        line["e2e"] = {"value": reduce_sum(pg, float(e_ev)) / e_wall, "unit": "events/s",
+                       "h2d_bytes_per_step": int(2 * n * net.stride * 4), "d2h_bytes_per_step": int(d2h),
+                       "steps": k, "path": "g4s_net_load_tables (pinned host) + g4s_net_reset + g4s_net_run "
+                                           "(raster recorded) + g4s_net_raster"}
+        e2e_net.close()
+        _lib.pinned_free(p_idx)
+        _lib.pinned_free(p_w)
+    else:
+        net.close()
+    if rank == 0 and ws == 1 and not a.no_cpu:
+        threads = os.cpu_count() or 1
+        v, st, dt = cpu_port_rate(n, nsyn, seed, drive, threads, min_seconds=12.0, max_steps=2000,
+                                  warm_steps=100)
+        line["cpu_baseline"] = {"value": v, "unit": "events/s", "cores": threads, "kind": "port",
+                                "sample": f"{st} simulation steps after 100 warm-up steps of the same network "
+                                          f"({dt:.1f} s), oracle OpenMP port"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -66,6 +66,8 @@ class NetInfo(C.Structure):
         ("last_algorithm", C.c_int32),
         ("persistent_blocks", C.c_int32),
         ("device_bytes", C.c_int64),
+        ("last_run_kernel_ms", C.c_double),
+        ("last_run_launches", C.c_int64),
     ]
 
 
@@ -74,6 +76,7 @@ _P = C.c_void_p
 SIGNATURES = [
     ("g4s_abi_version", C.c_int, []),
     ("g4s_last_error", C.c_char_p, []),
+    ("g4s_set_device", C.c_int, [C.c_int32]),
     ("g4s_net_create", C.c_int, [C.POINTER(NetDesc), C.POINTER(_P)]),
     ("g4s_net_create_from_tables", C.c_int, [C.POINTER(NetDesc), _P, _P, C.c_int32, C.POINTER(_P)]),
     ("g4s_net_load_tables", C.c_int, [_P, _P, _P, C.c_int32]),
@@ -88,13 +91,31 @@ SIGNATURES = [
     ("g4s_net_tables", C.c_int, [_P, C.c_int64, C.c_int64, _P, _P]),
     ("g4s_net_stats", C.c_int, [_P, _P, _P, _P]),
     ("g4s_net_set_barrier_timeout", C.c_int, [_P, C.c_uint64]),
+    ("g4s_net_set_geometry", C.c_int, [_P, C.c_int32]),
+    ("g4s_net_get_geometry", C.c_int, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int64)]),
     ("g4s_net_destroy", C.c_int, [_P]),
     ("g4s_inject_fault", C.c_int, [_P, C.c_int32]),
     ("g4s_net_write_results", C.c_int, [_P, C.c_char_p, _P, C.c_double, C.c_double]),
     ("g4s_run_protocol", C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_uint64,
                                    C.c_int32, C.c_char_p]),
     ("g4s_conn_glibc", C.c_int, [C.c_uint32, C.c_int32, C.c_int32, C.c_int32, _P, _P]),
+    ("g4s_pinned_alloc", C.c_int, [C.c_uint64, C.POINTER(_P)]),
+    ("g4s_pinned_free", C.c_int, [_P]),
 ]
+
+
+def pinned_empty(shape, dtype) -> tuple[np.ndarray, C.c_void_p]:
+    """A numpy array over page-locked host memory; free it with pinned_free(handle)."""
+    dt = np.dtype(dtype)
+    nbytes = int(np.prod(shape)) * dt.itemsize
+    p = C.c_void_p()
+    check(load().g4s_pinned_alloc(nbytes, C.byref(p)))
+    buf = (C.c_byte * nbytes).from_address(p.value)
+    return np.frombuffer(buf, dtype=dt).reshape(shape), p
+
+
+def pinned_free(p: C.c_void_p):
+    check(load().g4s_pinned_free(p))
 
 _lib = None
 

@@ -54,7 +54,9 @@ struct g4s_net {
   g4s_net_desc desc{};
   NetView v{};
   cudaStream_t stream = nullptr;
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr, ek0 = nullptr, ek1 = nullptr;
+  double last_kernel_ms = 0;
+  int64_t last_launches = 0;
   GridSync *gs = nullptr;
   double *d_stats = nullptr;
   int64_t chunk_steps = 0;
@@ -75,6 +77,16 @@ struct g4s_net {
   int last_alg = -1;
   DeliverShape shape;
   int barrier_stall = 0;  // injected: extra arrivals the next SKL launch waits for
+  // owner-computes SKL: geometry, per-row segment table, requested owner CTAs (0 = auto),
+  // and whether the tables satisfy the exactness bound of the split accumulation
+  OwnerGeom geo{};
+  bool geo_ready = false;
+  uint16_t *seg = nullptr;
+  size_t seg_bytes = 0;
+  int want_p = 0;
+  bool owner_ok = true;
+  bool tables_fit = false;
+  unsigned long long max_in = 0, max_mag = 0;
 };
 
 static std::atomic<int> g_fail_next_alloc{0};
@@ -96,12 +108,15 @@ static void free_net(g4s_net *n) {
   cudaFree(v.status);
   cudaFree(n->gs);
   cudaFree(n->d_stats);
+  cudaFree(n->seg);
   cudaFreeHost(n->h_counts);
   cudaFreeHost(n->h_base);
   cudaFreeHost(n->h_stamps);
   cudaFreeHost(n->h_raster);
   if (n->ev0) cudaEventDestroy(n->ev0);
   if (n->ev1) cudaEventDestroy(n->ev1);
+  if (n->ek0) cudaEventDestroy(n->ek0);
+  if (n->ek1) cudaEventDestroy(n->ek1);
   if (n->stream) cudaStreamDestroy(n->stream);
   delete n;
 }
@@ -112,6 +127,7 @@ static int validate(const g4s_net_desc *d) {
   if (!d) return set_error(G4S_ERR_INVALID, "null descriptor");
   if (d->n < 2 || d->n > (int64_t)INT32_MAX) return set_error(G4S_ERR_INVALID, "n must be in [2, 2^31)");
   if (d->nsyn < 1) return set_error(G4S_ERR_INVALID, "nsyn must be >= 1");
+  if (d->nsyn > kMaxSortedNsyn) return set_error(G4S_ERR_INVALID, "nsyn must be <= 16384");
   const int64_t maxsyn = d->self_loops ? d->n : d->n - 1;
   if (d->nsyn > maxsyn) return set_error(G4S_ERR_INVALID, "nsyn exceeds the number of possible targets");
   if (d->exc_permille < 0 || d->exc_permille > 1000) return set_error(G4S_ERR_INVALID, "exc_permille must be in [0, 1000]");
@@ -188,6 +204,7 @@ static int alloc_net(const g4s_net_desc *d, g4s_net **out) {
   }
   if ((e = cudaStreamCreateWithFlags(&n->stream, cudaStreamNonBlocking)) != cudaSuccess ||
       (e = cudaEventCreate(&n->ev0)) != cudaSuccess || (e = cudaEventCreate(&n->ev1)) != cudaSuccess ||
+      (e = cudaEventCreate(&n->ek0)) != cudaSuccess || (e = cudaEventCreate(&n->ek1)) != cudaSuccess ||
       (e = cudaMallocHost((void **)&n->h_counts, (size_t)cs * 4)) != cudaSuccess ||
       (e = cudaMallocHost((void **)&n->h_base, (size_t)cs * 8)) != cudaSuccess ||
       (e = cudaMallocHost((void **)&n->h_stamps, ((size_t)cs * 2 + 2) * 8)) != cudaSuccess) {
@@ -293,6 +310,92 @@ static int resolve_alg(g4s_net *n, int alg) {
   return alg;
 }
 
+// Geometry of the owner-computes kernel: p owner CTAs (at most the co-resident count, one
+// per SM), by default one per 2048 neurons (two neurons per thread per step), and the
+// currents plus the spike buffer of a slice within the shared-memory limit.  Returns
+// false if the network does not fit or its tables break the exactness bound of the split
+// accumulation (the global-atomic persistent kernel is used instead).
+static bool plan_owner(g4s_net *n, OwnerGeom *g) {
+  const NetView &v = n->v;
+  if (!n->tables_fit) return false;
+  const int64_t rc_cap = (int64_t)((kOwnerSmemLimit - 16) / 12);
+  int pmax = 0;
+  if (owner_max_blocks(owner_smem(std::min<int64_t>(rc_cap, v.n)), &pmax) != cudaSuccess || pmax < 1) {
+    (void)cudaGetLastError();
+    return false;
+  }
+  int64_t p = n->want_p > 0 ? n->want_p : (v.n + 2047) / 2048;
+  if (p < 1) p = 1;
+  if (p > pmax) p = pmax;
+  int64_t rc = (v.n + p - 1) / p;
+  if (rc > rc_cap) {
+    rc = (v.n + pmax - 1) / pmax;
+    p = (v.n + rc - 1) / rc;
+    if (rc > rc_cap) return false;
+  }
+  int pfit = 0;
+  if (owner_max_blocks(owner_smem(rc), &pfit) != cudaSuccess || pfit < p) {
+    (void)cudaGetLastError();
+    return false;
+  }
+  g->p = (int)p;
+  g->pad = 0;
+  g->rc = rc;
+  return true;
+}
+
+static int prepare_owner(g4s_net *n) {
+  if (n->geo_ready) return G4S_OK;
+  OwnerGeom g{};
+  if (!plan_owner(n, &g)) {
+    n->owner_ok = false;
+    return G4S_OK;
+  }
+  const size_t bytes = (size_t)n->v.n * (size_t)(g.p + 1) * sizeof(uint16_t);
+  if (bytes > n->seg_bytes) {
+    cudaFree(n->seg);
+    n->seg = nullptr;
+    n->device_bytes -= n->seg_bytes;
+    n->seg_bytes = 0;
+    cudaError_t e = cudaMalloc((void **)&n->seg, bytes);
+    if (e != cudaSuccess) return cuda_error(e, "segment table");
+    n->seg_bytes = bytes;
+    n->device_bytes += bytes;
+  }
+  G4S_CUDA(launch_segoff(n->v, g, n->seg, n->stream));
+  G4S_CUDA(cudaStreamSynchronize(n->stream));
+  n->geo = g;
+  n->geo_ready = true;
+  n->owner_ok = true;
+  return G4S_OK;
+}
+
+// Tables are kept with every row sorted by target (the pairs stay together); the
+// segment table of the owner-computes kernel is rebuilt on the next SKL run.  The
+// exactness bound of the split shared-memory accumulation is measured here: fewer than
+// 65536 synapses into any neuron and sum(|q| >> 16) + 1 over them below 2^31 - 2^20.
+static int finish_tables(g4s_net *n) {
+  G4S_CUDA(launch_sort_rows(n->v, n->stream));
+  n->geo_ready = false;
+  unsigned *cnt = nullptr;
+  unsigned long long *mag = nullptr, *out = nullptr;
+  cudaError_t e = cudaMalloc((void **)&cnt, (size_t)n->v.n * 4);
+  if (e == cudaSuccess) e = cudaMalloc((void **)&mag, (size_t)n->v.n * 8);
+  if (e == cudaSuccess) e = cudaMalloc((void **)&out, 16);
+  unsigned long long h[2] = {~0ull, ~0ull};
+  if (e == cudaSuccess) e = launch_inbound(n->v, cnt, mag, out, n->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(h, out, 16, cudaMemcpyDeviceToHost, n->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(n->stream);
+  cudaFree(cnt);
+  cudaFree(mag);
+  cudaFree(out);
+  if (e != cudaSuccess) return cuda_error(e, "table bound pass");
+  n->max_in = h[0];
+  n->max_mag = h[1];
+  n->tables_fit = h[0] < 65536ull && h[1] < (1ull << 31) - (1ull << 20);
+  return check_status(n, "row sort");
+}
+
 static int run_net(g4s_net *n, int32_t steps, int32_t alg_in) {
   if (steps < 0) return set_error(G4S_ERR_INVALID, "steps must be >= 0");
   if (alg_in < 0 || alg_in > kAlgAuto) return set_error(G4S_ERR_INVALID, "unknown algorithm");
@@ -300,30 +403,48 @@ static int run_net(g4s_net *n, int32_t steps, int32_t alg_in) {
   const int alg = resolve_alg(n, alg_in);
   NetView &v = n->v;
   if (n->shape.k_hint <= 0) n->shape.k_hint = (int)std::max<int64_t>(1, v.n / 20);
+  if (alg == kAlgSKL) {
+    int rc0 = prepare_owner(n);
+    if (rc0) return rc0;
+  }
+  const bool owner = alg == kAlgSKL && n->owner_ok && n->geo_ready;
   const auto w0 = std::chrono::steady_clock::now();
   G4S_CUDA(cudaEventRecord(n->ev0, n->stream));
-  int64_t remaining = steps, spikes = 0;
+  int64_t remaining = steps, spikes = 0, launches = 0;
+  double kernel_ms = 0.0;
   while (remaining > 0) {
     const int cs = (int)std::min<int64_t>(remaining, n->chunk_steps);
     const bool last_chunk = remaining == cs;
     G4S_CUDA(cudaMemsetAsync(v.counts, 0, (size_t)cs * sizeof(int), n->stream));
     G4S_CUDA(cudaMemsetAsync(v.stamps, 0, ((size_t)cs * 2 + 2) * 8, n->stream));
-    if (alg == kAlgSKL) {
-      G4S_CUDA(cudaMemsetAsync(n->gs, 0, sizeof(GridSync), n->stream));
+    if (alg == kAlgSKL) G4S_CUDA(cudaMemsetAsync(n->gs, 0, sizeof(GridSync), n->stream));
+    G4S_CUDA(cudaEventRecord(n->ek0, n->stream));
+    if (owner) {
+      G4S_CUDA(launch_owner(v, n->geo, n->seg, n->t_abs, cs, last_chunk, n->gs, n->barrier_ns, n->barrier_stall,
+                            n->stream));
+      n->barrier_stall = 0;
+      launches += 1;
+    } else if (alg == kAlgSKL) {
       G4S_CUDA(launch_persistent(v, n->t_abs, cs, last_chunk, n->gs, n->barrier_ns, n->shape.group,
                                  n->barrier_stall, n->stream));
       n->barrier_stall = 0;
+      launches += 1;
     } else {
       for (int lt = 0; lt < cs; ++lt) {
         G4S_CUDA(launch_update(v, n->t_abs, lt, last_chunk && lt == cs - 1, n->stream));
         G4S_CUDA(launch_deliver(v, lt, alg, n->shape, n->stream));
       }
+      launches += 2 * (int64_t)cs;
     }
+    G4S_CUDA(cudaEventRecord(n->ek1, n->stream));
     G4S_CUDA(cudaMemcpyAsync(n->h_counts, v.counts, (size_t)cs * 4, cudaMemcpyDeviceToHost, n->stream));
     G4S_CUDA(cudaMemcpyAsync(n->h_base, v.base, (size_t)cs * 8, cudaMemcpyDeviceToHost, n->stream));
     G4S_CUDA(cudaMemcpyAsync(n->h_stamps, v.stamps, (size_t)cs * 16, cudaMemcpyDeviceToHost, n->stream));
     int rc = check_status(n, alg == kAlgSKL ? "persistent step kernel" : "step kernels");
     if (rc) return rc;
+    float kms = 0.0f;
+    G4S_CUDA(cudaEventElapsedTime(&kms, n->ek0, n->ek1));
+    kernel_ms += kms;
     const int64_t chunk_total = (int64_t)n->h_base[cs - 1] + n->h_counts[cs - 1];
     if (n->desc.record_raster && chunk_total > 0) {
       G4S_CUDA(cudaMemcpyAsync(n->h_raster, v.raster, (size_t)chunk_total * 4, cudaMemcpyDeviceToHost, n->stream));
@@ -361,6 +482,8 @@ static int run_net(g4s_net *n, int32_t steps, int32_t alg_in) {
   n->last_spikes = spikes;
   n->total_spikes += spikes;
   n->last_alg = alg;
+  n->last_kernel_ms = kernel_ms;
+  n->last_launches = launches;
   return G4S_OK;
 }
 
@@ -437,6 +560,11 @@ int g4s_abi_version(void) { return G4S_ABI_VERSION; }
 
 const char *g4s_last_error(void) { return g_last_error.c_str(); }
 
+int g4s_set_device(int32_t device) {
+  G4S_CUDA(cudaSetDevice(device));
+  return G4S_OK;
+}
+
 int g4s_net_create(const g4s_net_desc *desc, g4s_net **out) {
   if (!out) return set_error(G4S_ERR_INVALID, "null output handle");
   *out = nullptr;
@@ -460,6 +588,7 @@ int g4s_net_create(const g4s_net_desc *desc, g4s_net **out) {
     cudaError_t e = launch_conngen(n->v, desc->self_loops, n->stream);
     if (e != cudaSuccess) rc = cuda_error(e, "connectivity kernel");
     if (!rc) rc = check_status(n, "connectivity kernel");
+    if (!rc) rc = finish_tables(n);
   }
   if (!rc) rc = reset_net(n);
   if (rc) {
@@ -500,7 +629,25 @@ int g4s_net_load_tables(g4s_net *n, const int32_t *idx, const float *w, int32_t 
                                             std::to_string(idx[k]) + " >= n");
   G4S_CUDA(cudaMemcpyAsync(const_cast<int *>(v.idx), idx, bytes, cudaMemcpyHostToDevice, n->stream));
   G4S_CUDA(cudaMemcpyAsync(const_cast<float *>(v.w), w, bytes, cudaMemcpyHostToDevice, n->stream));
-  G4S_CUDA(cudaStreamSynchronize(n->stream));
+  return finish_tables(n);
+}
+
+int g4s_net_set_geometry(g4s_net *n, int32_t owner_blocks) {
+  if (!n) return set_error(G4S_ERR_INVALID, "null handle");
+  if (owner_blocks < 0) return set_error(G4S_ERR_INVALID, "owner_blocks must be >= 0 (0 = automatic)");
+  n->want_p = owner_blocks;
+  n->geo_ready = false;
+  n->owner_ok = true;
+  return G4S_OK;
+}
+
+int g4s_net_get_geometry(g4s_net *n, int32_t *owner_blocks, int64_t *slice) {
+  if (!n) return set_error(G4S_ERR_INVALID, "null handle");
+  int rc = prepare_owner(n);
+  if (rc) return rc;
+  const bool ok = n->owner_ok && n->geo_ready;
+  if (owner_blocks) *owner_blocks = ok ? n->geo.p : 0;
+  if (slice) *slice = ok ? n->geo.rc : 0;
   return G4S_OK;
 }
 
@@ -528,6 +675,20 @@ int g4s_net_get_info(g4s_net *n, g4s_net_info *info) {
   info->last_algorithm = n->last_alg;
   info->persistent_blocks = persistent_blocks();
   info->device_bytes = (int64_t)n->device_bytes;
+  info->last_run_kernel_ms = n->last_kernel_ms;
+  info->last_run_launches = n->last_launches;
+  return G4S_OK;
+}
+
+int g4s_pinned_alloc(uint64_t bytes, void **out) {
+  if (!out) return set_error(G4S_ERR_INVALID, "null output pointer");
+  *out = nullptr;
+  G4S_CUDA(cudaMallocHost(out, bytes ? (size_t)bytes : 16));
+  return G4S_OK;
+}
+
+int g4s_pinned_free(void *p) {
+  if (p) G4S_CUDA(cudaFreeHost(p));
   return G4S_OK;
 }
 

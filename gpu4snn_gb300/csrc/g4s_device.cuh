@@ -79,16 +79,40 @@ __device__ __forceinline__ float pm1_from24(uint32_t k) {
   return __fmul_rn(__int2float_rn((int)(2u * k + 1u) - 0x1000000), kTwoM24);
 }
 
-// Standard normal for (neuron, step) by Marsaglia's polar method; four candidate pairs
-// per Philox call, up to eight calls (counter word 2), z = 0 if all 32 are rejected.
-// Replaces curand_normal (gpu4snn.cu:358).
-__device__ __forceinline__ float normal(uint64_t seed, uint64_t neuron, uint64_t step) {
-  for (uint64_t attempt = 0; attempt < 8; ++attempt) {
-    const U64x4 o = philox(seed, kStreamNoise, neuron, step, attempt);
+// Philox4x32-10 (same paper), the cheaper generator of the per-step thalamic drive:
+// 32x32->64 products instead of 64x64->128 ones.
+__device__ __forceinline__ uint4 philox32(uint32_t k0, uint32_t k1, uint32_t c0, uint32_t c1, uint32_t c2,
+                                          uint32_t c3) {
 #pragma unroll
-    for (int p = 0; p < 4; ++p) {
-      const float x = pm1_from24((uint32_t)(o.x[p] >> 40));
-      const float y = pm1_from24((uint32_t)(o.x[p] >> 8) & 0xFFFFFFu);
+  for (int r = 0; r < 10; ++r) {
+    if (r) {
+      k0 += 0x9E3779B9u;
+      k1 += 0xBB67AE85u;
+    }
+    const uint32_t lo0 = 0xD2511F53u * c0, hi0 = __umulhi(0xD2511F53u, c0);
+    const uint32_t lo1 = 0xCD9E8D57u * c2, hi1 = __umulhi(0xCD9E8D57u, c2);
+    const uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+    c0 = n0;
+    c1 = lo1;
+    c2 = n2;
+    c3 = lo0;
+  }
+  return make_uint4(c0, c1, c2, c3);
+}
+
+// Standard normal for (neuron, step) by Marsaglia's polar method: one Philox4x32-10 call
+// (key = seed words, counter = (neuron, step, attempt, 4)) gives two candidate pairs from
+// the top 24 bits of words (0,1) and (2,3); up to 16 calls, z = 0 if all 32 pairs are
+// rejected.  Replaces curand_normal (gpu4snn.cu:358).
+__device__ __forceinline__ float normal(uint64_t seed, uint64_t neuron, uint64_t step) {
+  const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+  for (uint32_t attempt = 0; attempt < 16; ++attempt) {
+    const uint4 o = philox32(k0, k1, (uint32_t)neuron, (uint32_t)step, attempt, (uint32_t)kStreamNoise);
+    const uint32_t w[4] = {o.x, o.y, o.z, o.w};
+#pragma unroll
+    for (int p = 0; p < 2; ++p) {
+      const float x = pm1_from24(w[2 * p] >> 8);
+      const float y = pm1_from24(w[2 * p + 1] >> 8);
       const float s = __fadd_rn(__fmul_rn(x, x), __fmul_rn(y, y));
       if (s < 1.0f) {
         const float q = __fdiv_rn(__fmul_rn(-2.0f, log_pos(s)), s);
@@ -214,7 +238,6 @@ __device__ __forceinline__ bool grid_barrier(GridSync *gs, unsigned nblocks, uns
         ok = 0;
         break;
       }
-      __nanosleep(20);
     }
     if (ok && ld_relaxed(&gs->error) != 0) ok = 0;
     __threadfence();

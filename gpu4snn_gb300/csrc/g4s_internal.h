@@ -33,6 +33,18 @@ cudaError_t launch_persistent(const NetView &v, int64_t t_abs0, int nsteps, bool
 cudaError_t launch_stats(const NetView &v, double *out, cudaStream_t s);
 int persistent_blocks();
 
+// Owner-computes SKL (g4s_owner.cu).
+constexpr int kMaxSortedNsyn = 16384;          // rows are sorted in shared memory
+constexpr size_t kOwnerSmemLimit = 200 * 1024; // shared memory per CTA for currents + spikes
+cudaError_t launch_sort_rows(const NetView &v, cudaStream_t s);
+cudaError_t launch_segoff(const NetView &v, const OwnerGeom &geo, uint16_t *seg, cudaStream_t s);
+cudaError_t launch_owner(const NetView &v, const OwnerGeom &geo, const uint16_t *seg, int64_t t_abs0, int nsteps,
+                         bool last_chunk, GridSync *gs, unsigned long long limit_ns, int stall, cudaStream_t s);
+cudaError_t launch_inbound(const NetView &v, unsigned *cnt, unsigned long long *mag, unsigned long long *out,
+                           cudaStream_t s);
+cudaError_t owner_max_blocks(size_t smem, int *out);
+size_t owner_smem(int64_t rc);
+
 // Error reporting (thread-local message behind g4s_last_error()).
 int set_error(int code, const std::string &msg);
 int cuda_error(cudaError_t e, const char *what);

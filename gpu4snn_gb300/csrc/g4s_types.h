@@ -56,4 +56,12 @@ struct NetView {
   int *status;      // device error word (kErr*Code)
 };
 
+// Launch geometry of the owner-computes SKL kernel: p CTAs, CTA k owns the neurons
+// [k rc, (k+1) rc).
+struct OwnerGeom {
+  int p;       // owner CTAs
+  int pad;
+  int64_t rc;  // neurons per CTA slice
+};
+
 }  // namespace g4s

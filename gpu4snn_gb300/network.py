@@ -85,6 +85,16 @@ class Network:
     def inject_fault(self, kind: int):
         check(load().g4s_inject_fault(self._h, kind))
 
+    def set_geometry(self, owner_blocks: int = 0):
+        """SKL owner CTAs (0 = automatic)."""
+        check(load().g4s_net_set_geometry(self._h, owner_blocks))
+
+    def geometry(self) -> tuple[int, int]:
+        """(owner CTAs, neurons per CTA) of the SKL kernel; (0, 0) on the fallback kernel."""
+        p, rc = C.c_int32(), C.c_int64()
+        check(load().g4s_net_get_geometry(self._h, C.byref(p), C.byref(rc)))
+        return p.value, rc.value
+
     def load_tables(self, idx: np.ndarray, w: np.ndarray):
         idx = np.ascontiguousarray(idx, dtype=np.int32)
         w = np.ascontiguousarray(w, dtype=np.float32)

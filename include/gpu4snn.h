@@ -76,10 +76,15 @@ typedef struct g4s_net_info {
   int32_t last_algorithm;    /* scheme the last run used (AUTO resolved)                */
   int32_t persistent_blocks; /* grid of the SKL kernel                                  */
   int64_t device_bytes;      /* device memory held by the handle                        */
+  double last_run_kernel_ms; /* CUDA-event time of the step kernels alone, last run     */
+  int64_t last_run_launches; /* kernel launches of the last run                         */
 } g4s_net_info;
 
 int g4s_abi_version(void);
 const char *g4s_last_error(void);
+/* CUDA device of the calling thread for subsequent handles (the reference picks it with
+ * findCudaDevice, gpu4snn.cu:818). */
+int g4s_set_device(int32_t device);
 
 /* Allocation + initNeuron + connectivity (gpu4snn.cu:750-911, 1094). */
 int g4s_net_create(const g4s_net_desc *desc, g4s_net **out);
@@ -113,6 +118,14 @@ int g4s_net_stats(g4s_net *net, double *rate_hz, double *isi_cv, int64_t *total_
 /* Grid-barrier time limit of the SKL kernel in ns (default 2 s); 0 makes every barrier
  * give up at once (used to test the timeout path). */
 int g4s_net_set_barrier_timeout(g4s_net *net, uint64_t ns);
+/* Geometry of the SKL kernel (the reference sizes its persistent grids from occupancy,
+ * gpu4snn.cu:1066-1076): `owner_blocks` CTAs, each owning a contiguous slice of target
+ * neurons whose currents stay in its shared memory; 0 = automatic.  get_geometry reports
+ * the geometry in use (zeros when the network is too large for shared-memory ownership,
+ * or its tables exceed the exact-accumulation bound, and the global-atomic persistent
+ * kernel runs instead) and the neurons per CTA. */
+int g4s_net_set_geometry(g4s_net *net, int32_t owner_blocks);
+int g4s_net_get_geometry(g4s_net *net, int32_t *owner_blocks, int64_t *slice);
 int g4s_net_destroy(g4s_net *net);
 
 /* Host-side fault injection for failure-detection tests (nothing faults the GPU):
@@ -136,6 +149,11 @@ int g4s_net_write_results(g4s_net *net, const char *dir, const float *init_state
  * network and write Results/N{n}Nsyn{nsyn}Regime{mode}Alg{alg}/ under results_root. */
 int g4s_run_protocol(int32_t n, int32_t nsyn, int32_t iterations, int32_t algorithm, int32_t mode, uint64_t seed,
                      int32_t conn_law, const char *results_root);
+
+/* Page-locked host buffers for fast table uploads and raster downloads (the reference
+ * copies from pageable malloc memory, gpu4snn.cu:863-866, 910-911). */
+int g4s_pinned_alloc(uint64_t bytes, void **out);
+int g4s_pinned_free(void *p);
 
 /* The reference's host table generator with glibc rand() after srand(seed)
  * (gpu4snn.cu:873-898), into [n][stride] host buffers (padding: -1 / 0). */

@@ -56,6 +56,32 @@ void g4o_philox4x64_10(const uint64_t ctr[4], const uint64_t key[2], uint64_t ou
   out[3] = c3;
 }
 
+/* Philox4x32-10 (same paper): (hi0,lo0) = M0*c0, (hi1,lo1) = M1*c2 in 32x32->64,
+ * c' = (hi1^c1^k0, lo1, hi0^c3^k1, lo0), key bumped by the 32-bit Weyl constants.
+ * Pinned against the Philox4x32-10 host generator of the CUDA toolkit's cuRAND. */
+void g4o_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
+  uint32_t c0 = ctr[0], c1 = ctr[1], c2 = ctr[2], c3 = ctr[3];
+  uint32_t k0 = key[0], k1 = key[1];
+  for (int r = 0; r < 10; ++r) {
+    if (r) {
+      k0 += 0x9E3779B9u;
+      k1 += 0xBB67AE85u;
+    }
+    const uint64_t p0 = (uint64_t)0xD2511F53u * c0, p1 = (uint64_t)0xCD9E8D57u * c2;
+    const uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+    const uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+    const uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+    c0 = n0;
+    c1 = lo1;
+    c2 = n2;
+    c3 = lo0;
+  }
+  out[0] = c0;
+  out[1] = c1;
+  out[2] = c2;
+  out[3] = c3;
+}
+
 static inline void philox(uint64_t seed, uint64_t stream, uint64_t c0, uint64_t c1, uint64_t c2,
                           uint64_t out[4]) {
   const uint64_t ctr[4] = {c0, c1, c2, 0};
@@ -108,21 +134,24 @@ float g4o_logf(float x) {
 }
 
 /* ---------------------------------------------------------------------------------
- * Standard normal for (neuron, step): Marsaglia's polar method.  One Philox call gives
- * four (x, y) candidate pairs; x, y are odd multiples of 2^-24 in (-1, 1) (exact in
- * binary32).  Accept s = x^2 + y^2 < 1, z = x * sqrt(-2 log(s) / s).  Up to 8 calls
- * (attempt = counter word 2); if all 32 pairs are rejected (p ~ 1e-21) z = 0.
- * Replaces curand_normal at gpu4snn.cu:358.
+ * Standard normal for (neuron, step): Marsaglia's polar method.  One Philox4x32-10 call
+ * with key (seed low, seed high) and counter (neuron, step, attempt, stream 4) gives two
+ * (x, y) candidate pairs from the top 24 bits of words (0,1) and (2,3); x, y are odd
+ * multiples of 2^-24 in (-1, 1) (exact in binary32).  Accept s = x^2 + y^2 < 1,
+ * z = x * sqrt(-2 log(s) / s).  Up to 16 calls; if all 32 pairs are rejected
+ * (p ~ 1e-21) z = 0.  Replaces curand_normal at gpu4snn.cu:358.
  * ------------------------------------------------------------------------------- */
 static inline float pm1_from24(uint32_t k) { return (float)((int32_t)(2u * k + 1u) - 0x1000000) * 0x1p-24f; }
 
 float g4o_normal(uint64_t seed, uint64_t neuron, uint64_t step) {
-  for (uint64_t attempt = 0; attempt < 8; ++attempt) {
-    uint64_t o[4];
-    philox(seed, G4O_STREAM_NOISE, neuron, step, attempt, o);
-    for (int p = 0; p < 4; ++p) {
-      float x = pm1_from24((uint32_t)(o[p] >> 40));
-      float y = pm1_from24((uint32_t)(o[p] >> 8) & 0xFFFFFFu);
+  const uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+  for (uint32_t attempt = 0; attempt < 16; ++attempt) {
+    const uint32_t ctr[4] = {(uint32_t)neuron, (uint32_t)step, attempt, (uint32_t)G4O_STREAM_NOISE};
+    uint32_t o[4];
+    g4o_philox4x32_10(ctr, key, o);
+    for (int p = 0; p < 2; ++p) {
+      float x = pm1_from24(o[2 * p] >> 8);
+      float y = pm1_from24(o[2 * p + 1] >> 8);
       float xx = x * x;
       float yy = y * y;
       float s = xx + yy;

@@ -37,7 +37,7 @@ extern "C" {
 #define G4O_STREAM_CONN 1u   /* connectivity target draws,  ctr = (row, draw block, 0, 0) */
 #define G4O_STREAM_WEIGHT 2u /* connectivity weights,      ctr = (row, slot/4, 0, 0)     */
 #define G4O_STREAM_PARAM 3u  /* neuron parameter r,        ctr = (neuron, 0, 0, 0)       */
-#define G4O_STREAM_NOISE 4u  /* thalamic noise,            ctr = (neuron, step, attempt, 0) */
+#define G4O_STREAM_NOISE 4u  /* thalamic noise, Philox4x32: ctr = (neuron, step, attempt, 4) */
 
 #define G4O_FP32 0
 #define G4O_FP64 1
@@ -55,6 +55,7 @@ typedef struct g4o_desc {
 
 /* ---- random numbers ---------------------------------------------------------- */
 void g4o_philox4x64_10(const uint64_t ctr[4], const uint64_t key[2], uint64_t out[4]);
+void g4o_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
 float g4o_logf(float x);
 float g4o_normal(uint64_t seed, uint64_t neuron, uint64_t step);
 float g4o_param_r(uint64_t seed, uint64_t neuron);

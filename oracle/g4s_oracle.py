@@ -50,6 +50,7 @@ def lib():
         L = C.CDLL(LIB_PATH)
         p = C.c_void_p
         L.g4o_philox4x64_10.argtypes = [p, p, p]
+        L.g4o_philox4x32_10.argtypes = [p, p, p]
         L.g4o_logf.argtypes = [C.c_float]
         L.g4o_logf.restype = C.c_float
         L.g4o_normal.argtypes = [C.c_uint64, C.c_uint64, C.c_uint64]
@@ -91,6 +92,14 @@ def philox4x64_10(ctr, key) -> np.ndarray:
     k = np.asarray(key, dtype=np.uint64)
     out = np.zeros(4, dtype=np.uint64)
     lib().g4o_philox4x64_10(_ptr(c), _ptr(k), _ptr(out))
+    return out
+
+
+def philox4x32_10(ctr, key) -> np.ndarray:
+    c = np.asarray(ctr, dtype=np.uint32)
+    k = np.asarray(key, dtype=np.uint32)
+    out = np.zeros(4, dtype=np.uint32)
+    lib().g4o_philox4x32_10(_ptr(c), _ptr(k), _ptr(out))
     return out
 
 

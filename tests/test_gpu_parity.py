@@ -13,14 +13,25 @@ def oracle_tables(O, n, nsyn, seed, self_loops=0):
     return d, O.conn_philox(d)
 
 
+def sorted_rows(idx, w):
+    """The library keeps each row sorted by target (unused slots, negative, last); the
+    oracle's rows are in draw order.  Same pairs, same order after this."""
+    order = np.argsort(idx.view(np.uint32), axis=1, kind="stable")
+    return np.take_along_axis(idx, order, 1), np.take_along_axis(w, order, 1)
+
+
+def same_tables(gi, gw, oi, ow):
+    si, sw = sorted_rows(oi, ow)
+    return np.array_equal(gi, si) and np.array_equal(gw.view(np.uint32), sw.view(np.uint32))
+
+
 @pytest.mark.parametrize("n,nsyn,seed,self_loops", [(2500, 1000, 1, 0), (1000, 999, 5, 0), (300, 37, 9, 0),
                                                     (257, 257, 11, 1), (5000, 3, 2, 0)])
 def test_tables_bit_exact(g4s, oracle, n, nsyn, seed, self_loops):
     _, (idx, w) = oracle_tables(oracle, n, nsyn, seed, self_loops)
     with g4s.Network(n, nsyn, seed=seed, self_loops=bool(self_loops)) as net:
         gi, gw = net.tables()
-    assert np.array_equal(gi, idx)
-    assert np.array_equal(gw.view(np.uint32), w.view(np.uint32))
+    assert same_tables(gi, gw, idx, w)
 
 
 def test_tables_large_sampled_rows(g4s, oracle):
@@ -30,7 +41,7 @@ def test_tables_large_sampled_rows(g4s, oracle):
         for row0 in (0, 1, 49_999, 79_999, 80_000, n - 3):
             gi, gw = net.tables(row0, 3)
             oi, ow = oracle.conn_philox(d, row0, 3)
-            assert np.array_equal(gi, oi) and np.array_equal(gw.view(np.uint32), ow.view(np.uint32))
+            assert same_tables(gi, gw, oi, ow)
 
 
 def compare_state(net, sim):
@@ -110,7 +121,7 @@ def test_glibc_tables_on_gpu(g4s, oracle):
     sim.run(100, threads=8)
     with g4s.Network(n, nsyn, seed=seed, self_loops=True, conn_law=g4s.CONN_GLIBC) as net:
         gi, gw = net.tables()
-        assert np.array_equal(gi, idx) and np.array_equal(gw.view(np.uint32), w.view(np.uint32))
+        assert same_tables(gi, gw, idx, w)
         net.run(100, 3)
         assert np.array_equal(np.stack(net.raster()), np.stack(sim.raster()))
         compare_state(net, sim)
@@ -136,3 +147,55 @@ def test_barrier_timeout_is_reported(g4s, oracle):
         sim = oracle.Sim(d, idx, w)
         sim.run(40)
         assert np.array_equal(np.stack(net.raster()), np.stack(sim.raster()))
+
+
+@pytest.mark.parametrize("p,n", [(1, 2500), (2, 2500), (3, 3001), (7, 5003), (152, 4099), (0, 20011), (40, 9000)])
+def test_owner_geometries(g4s, oracle, p, n):
+    """The owner-computes SKL kernel under forced geometries (one CTA, odd counts, more
+    CTAs than 2048-neuron slices, slices that do not divide N) against the oracle."""
+    nsyn, seed = 300, 21
+    d, (idx, w) = oracle_tables(oracle, n, nsyn, seed)
+    sim = oracle.Sim(d, idx, w)
+    sim.run(120, threads=8)
+    with g4s.Network(n, nsyn, seed=seed) as net:
+        net.set_geometry(p)
+        gp, rc = net.geometry()
+        assert (p == 0 or gp == p) and rc > 0
+        net.run(70, 4)
+        net.run(50, 4)
+        assert np.array_equal(np.stack(net.raster()), np.stack(sim.raster()))
+        compare_state(net, sim)
+
+
+def test_uploaded_tables_with_holes(g4s, oracle):
+    """Caller tables may leave slots unused (negative target) anywhere in a row."""
+    n, nsyn, seed = 3000, 200, 8
+    d, (idx, w) = oracle_tables(oracle, n, nsyn, seed)
+    rng = np.random.default_rng(0)
+    holes = rng.random(idx.shape) < 0.1
+    idx = idx.copy()
+    idx[holes] = -1
+    sim = oracle.Sim(d, idx, w)
+    sim.run(100, threads=8)
+    for alg in (2, 4):
+        with g4s.Network(n, nsyn, seed=seed, tables=(idx, w)) as net:
+            gi, gw = net.tables()
+            valid = gi >= 0
+            assert valid.sum() == (idx >= 0).sum()
+            net.run(100, alg)
+            assert np.array_equal(np.stack(net.raster()), np.stack(sim.raster()))
+            compare_state(net, sim)
+
+
+def test_owner_large_network(g4s, oracle):
+    """N=100,000, Nsyn=1000 (the scaled configuration) on the full GPU: many clusters."""
+    n, nsyn, seed = 100_000, 1000, 2
+    d, (idx, w) = oracle_tables(oracle, n, nsyn, seed)
+    sim = oracle.Sim(d, idx, w)
+    sim.run(200, threads=16)
+    with g4s.Network(n, nsyn, seed=seed) as net:
+        p, rc = net.geometry()
+        assert p > 1
+        net.run(200, 4)
+        assert np.array_equal(np.stack(net.raster()), np.stack(sim.raster()))
+        compare_state(net, sim)
