@@ -43,6 +43,7 @@ WORKLOADS = {
     "n250k_s10k": (250_000, 10_000, 500, 1.0, 4),
     "n2500": (2500, 1000, 2000, 1.0, 1),
     "n25k": (25_000, 1000, 500, 1.0, 5),  # small profiling case: 0.2 GB of tables, still > L2
+    "n300k": (300_000, 1000, 50, 1.0, 6),  # profiling case for large-N delivery: 2.4 GB of tables
 }
 # algorithmic bytes: delivery = spikes x Nsyn x (4 B target + 4 B weight); update per
 # neuron and step = v,u read+write (16) + a,b,c,d (16) + current read (8)

@@ -93,6 +93,7 @@ SIGNATURES = [
     ("g4s_net_set_barrier_timeout", C.c_int, [_P, C.c_uint64]),
     ("g4s_net_set_geometry", C.c_int, [_P, C.c_int32]),
     ("g4s_net_get_geometry", C.c_int, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int64)]),
+    ("g4s_nets_run", C.c_int, [_P, _P, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_int64)]),
     ("g4s_net_destroy", C.c_int, [_P]),
     ("g4s_inject_fault", C.c_int, [_P, C.c_int32]),
     ("g4s_net_write_results", C.c_int, [_P, C.c_char_p, _P, C.c_double, C.c_double]),

@@ -16,6 +16,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <fstream>
+#include <memory>
 #include <new>
 #include <string>
 #include <vector>
@@ -47,6 +48,50 @@ int cuda_error(cudaError_t e, const char *what) {
     if (e_ != cudaSuccess) return cuda_error(e_, #call); \
   } while (0)
 
+struct TeamLaunch {
+  TeamItem *d_items = nullptr, *h_items = nullptr;
+  int2 *d_slots = nullptr, *h_slots = nullptr;
+  int *d_ctl = nullptr, *h_ctl = nullptr;  // [0] slot count, [1] queue head
+  int cap_items = 0, cap_slots = 0;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  void release() {
+    cudaFree(d_items);
+    cudaFree(d_slots);
+    cudaFree(d_ctl);
+    cudaFreeHost(h_items);
+    cudaFreeHost(h_slots);
+    cudaFreeHost(h_ctl);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    *this = TeamLaunch{};
+  }
+  int reserve(int items, int slots) {
+    if (!e0 && (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess))
+      return set_error(G4S_ERR_CUDA, "team launch events");
+    if (!d_ctl && (cudaMalloc((void **)&d_ctl, 16) != cudaSuccess || cudaMallocHost((void **)&h_ctl, 16) != cudaSuccess))
+      return set_error(G4S_ERR_NOMEM, "team launch control words");
+    if (items > cap_items) {
+      cudaFree(d_items);
+      cudaFreeHost(h_items);
+      d_items = h_items = nullptr;
+      if (cudaMalloc((void **)&d_items, sizeof(TeamItem) * items) != cudaSuccess ||
+          cudaMallocHost((void **)&h_items, sizeof(TeamItem) * items) != cudaSuccess)
+        return set_error(G4S_ERR_NOMEM, "team items");
+      cap_items = items;
+    }
+    if (slots > cap_slots) {
+      cudaFree(d_slots);
+      cudaFreeHost(h_slots);
+      d_slots = h_slots = nullptr;
+      if (cudaMalloc((void **)&d_slots, sizeof(int2) * slots) != cudaSuccess ||
+          cudaMallocHost((void **)&h_slots, sizeof(int2) * slots) != cudaSuccess)
+        return set_error(G4S_ERR_NOMEM, "team slots");
+      cap_slots = slots;
+    }
+    return G4S_OK;
+  }
+};
+
 // ---------------------------------------------------------------------------------------
 // Handle.
 // ---------------------------------------------------------------------------------------
@@ -59,7 +104,8 @@ struct g4s_net {
   int64_t last_launches = 0;
   GridSync *gs = nullptr;
   double *d_stats = nullptr;
-  int64_t chunk_steps = 0;
+  int64_t chunk_steps = 0;   // steps per chunk of the team kernel
+  int64_t chunk_legacy = 0;  // steps per chunk of the other kernels (raster = spike list)
   int64_t t_abs = 0;
   unsigned long long barrier_ns = 2000000000ull;
   size_t device_bytes = 0;
@@ -77,16 +123,20 @@ struct g4s_net {
   int last_alg = -1;
   DeliverShape shape;
   int barrier_stall = 0;  // injected: extra arrivals the next SKL launch waits for
-  // owner-computes SKL: geometry, per-row segment table, requested owner CTAs (0 = auto),
-  // and whether the tables satisfy the exactness bound of the split accumulation
-  OwnerGeom geo{};
-  bool geo_ready = false;
+  // SKL team kernel: team size and slice, per-step spike lists, per-row segment table,
+  // requested team size (0 = auto), whether the tables satisfy the exactness bound of the
+  // split accumulation, and the launch buffers of the handle's own runs
+  int team_p = 0;
+  int64_t team_rc = 0;
+  bool team_ready = false;
+  bool team_ok = true;
+  int *list = nullptr;
   uint16_t *seg = nullptr;
   size_t seg_bytes = 0;
   int want_p = 0;
-  bool owner_ok = true;
   bool tables_fit = false;
   unsigned long long max_in = 0, max_mag = 0;
+  TeamLaunch launch;
 };
 
 static std::atomic<int> g_fail_next_alloc{0};
@@ -109,6 +159,8 @@ static void free_net(g4s_net *n) {
   cudaFree(n->gs);
   cudaFree(n->d_stats);
   cudaFree(n->seg);
+  cudaFree(n->list);
+  n->launch.release();
   cudaFreeHost(n->h_counts);
   cudaFreeHost(n->h_base);
   cudaFreeHost(n->h_stamps);
@@ -171,13 +223,19 @@ static int alloc_net(const g4s_net_desc *d, g4s_net **out) {
   v.seed = d->seed;
   set_drive(n);
   const size_t N = (size_t)d->n, S = (size_t)v.stride;
-  // chunk: a raster buffer that holds every neuron firing at every step of the chunk
-  int64_t budget = d->raster_budget_bytes > 0 ? d->raster_budget_bytes : (int64_t)1 << 30;
+  // chunk: a raster buffer that holds every neuron firing at every step of the chunk (the
+  // host-driven schemes and the fallback kernel use it as the spike list).  The team
+  // kernel keeps its spike lists elsewhere, so when the raster is not recorded its chunk
+  // is bounded only by the per-step arrays.
+  const int64_t dflt = d->record_raster ? ((int64_t)1 << 30) : ((int64_t)64 << 20);
+  int64_t budget = d->raster_budget_bytes > 0 ? d->raster_budget_bytes : dflt;
   int64_t cs = budget / (int64_t)(4 * N);
   if (cs < 1) cs = 1;
   if (cs > 100000) cs = 100000;
-  n->chunk_steps = cs;
+  n->chunk_legacy = cs;
+  n->chunk_steps = d->record_raster ? cs : 16384;
   v.raster_cap = cs * (int64_t)N;
+  cs = std::max<int64_t>(cs, n->chunk_steps);
   size_t free_b = 0, total_b = 0;
   cudaError_t e = cudaMemGetInfo(&free_b, &total_b);
   if (e != cudaSuccess) {
@@ -218,7 +276,11 @@ static int alloc_net(const g4s_net_desc *d, g4s_net **out) {
       return cuda_error(e, "pinned raster staging");
     }
   }
-  cudaMemsetAsync(v.status, 0, sizeof(int), n->stream);
+  if ((e = cudaMemsetAsync(v.status, 0, sizeof(int), n->stream)) != cudaSuccess ||
+      (e = cudaMemsetAsync(n->gs, 0, sizeof(GridSync), n->stream)) != cudaSuccess) {
+    free_net(n);
+    return cuda_error(e, "clearing status words");
+  }
   *out = n;
   return G4S_OK;
 }
@@ -310,21 +372,23 @@ static int resolve_alg(g4s_net *n, int alg) {
   return alg;
 }
 
-// Geometry of the owner-computes kernel: p owner CTAs (at most the co-resident count, one
-// per SM), by default one per 2048 neurons (two neurons per thread per step), and the
-// currents plus the spike buffer of a slice within the shared-memory limit.  Returns
-// false if the network does not fit or its tables break the exactness bound of the split
-// accumulation (the global-atomic persistent kernel is used instead).
-static bool plan_owner(g4s_net *n, OwnerGeom *g) {
+// ---------------------------------------------------------------------------------------
+// Team geometry of one network for the SKL team kernel: p CTAs (at most the co-resident
+// count, one per SM), by default one per 2048 neurons (two neurons per thread per step),
+// and the currents plus the spike buffer of a slice within the shared-memory limit.
+// Returns false if the network does not fit or its tables break the exactness bound of
+// the split accumulation (the global-atomic persistent kernel is used instead).
+// ---------------------------------------------------------------------------------------
+static bool plan_team(g4s_net *n, int want, int *p_out, int64_t *rc_out) {
   const NetView &v = n->v;
   if (!n->tables_fit) return false;
-  const int64_t rc_cap = (int64_t)((kOwnerSmemLimit - 16) / 12);
+  const int64_t rc_cap = (int64_t)((kTeamSmemLimit - 16) / 12);
   int pmax = 0;
-  if (owner_max_blocks(owner_smem(std::min<int64_t>(rc_cap, v.n)), &pmax) != cudaSuccess || pmax < 1) {
+  if (team_max_blocks(team_smem(std::min<int64_t>(rc_cap, v.n)), &pmax) != cudaSuccess || pmax < 1) {
     (void)cudaGetLastError();
     return false;
   }
-  int64_t p = n->want_p > 0 ? n->want_p : (v.n + 2047) / 2048;
+  int64_t p = want > 0 ? want : (v.n + 2047) / 2048;
   if (p < 1) p = 1;
   if (p > pmax) p = pmax;
   int64_t rc = (v.n + p - 1) / p;
@@ -334,49 +398,59 @@ static bool plan_owner(g4s_net *n, OwnerGeom *g) {
     if (rc > rc_cap) return false;
   }
   int pfit = 0;
-  if (owner_max_blocks(owner_smem(rc), &pfit) != cudaSuccess || pfit < p) {
+  if (team_max_blocks(team_smem(rc), &pfit) != cudaSuccess || pfit < p) {
     (void)cudaGetLastError();
     return false;
   }
-  g->p = (int)p;
-  g->pad = 0;
-  g->rc = rc;
+  *p_out = (int)p;
+  *rc_out = rc;
   return true;
 }
 
-static int prepare_owner(g4s_net *n) {
-  if (n->geo_ready) return G4S_OK;
-  OwnerGeom g{};
-  if (!plan_owner(n, &g)) {
-    n->owner_ok = false;
+// Team geometry, the per-step spike lists and, for teams of more than one CTA, the
+// per-row segment table.
+static int prepare_team(g4s_net *n) {
+  if (n->team_ready) return G4S_OK;
+  int p = 0;
+  int64_t rc = 0;
+  if (!plan_team(n, n->want_p, &p, &rc)) {
+    n->team_ok = false;
     return G4S_OK;
   }
-  const size_t bytes = (size_t)n->v.n * (size_t)(g.p + 1) * sizeof(uint16_t);
-  if (bytes > n->seg_bytes) {
-    cudaFree(n->seg);
-    n->seg = nullptr;
-    n->device_bytes -= n->seg_bytes;
-    n->seg_bytes = 0;
-    cudaError_t e = cudaMalloc((void **)&n->seg, bytes);
-    if (e != cudaSuccess) return cuda_error(e, "segment table");
-    n->seg_bytes = bytes;
-    n->device_bytes += bytes;
+  if (!n->list) {
+    cudaError_t e = cudaMalloc((void **)&n->list, (size_t)n->v.n * 2 * sizeof(int));
+    if (e != cudaSuccess) return cuda_error(e, "spike lists");
+    n->device_bytes += (size_t)n->v.n * 2 * sizeof(int);
   }
-  G4S_CUDA(launch_segoff(n->v, g, n->seg, n->stream));
-  G4S_CUDA(cudaStreamSynchronize(n->stream));
-  n->geo = g;
-  n->geo_ready = true;
-  n->owner_ok = true;
+  if (p > 1) {
+    const size_t bytes = (size_t)n->v.n * (size_t)(p + 1) * sizeof(uint16_t);
+    if (bytes > n->seg_bytes) {
+      cudaFree(n->seg);
+      n->seg = nullptr;
+      n->device_bytes -= n->seg_bytes;
+      n->seg_bytes = 0;
+      cudaError_t e = cudaMalloc((void **)&n->seg, bytes);
+      if (e != cudaSuccess) return cuda_error(e, "segment table");
+      n->seg_bytes = bytes;
+      n->device_bytes += bytes;
+    }
+    G4S_CUDA(launch_segoff(n->v, p, rc, n->seg, n->stream));
+    G4S_CUDA(cudaStreamSynchronize(n->stream));
+  }
+  n->team_p = p;
+  n->team_rc = rc;
+  n->team_ready = true;
+  n->team_ok = true;
   return G4S_OK;
 }
 
 // Tables are kept with every row sorted by target (the pairs stay together); the
-// segment table of the owner-computes kernel is rebuilt on the next SKL run.  The
-// exactness bound of the split shared-memory accumulation is measured here: fewer than
-// 65536 synapses into any neuron and sum(|q| >> 16) + 1 over them below 2^31 - 2^20.
+// segment table of the team kernel is rebuilt on the next SKL run.  The exactness bound
+// of the split shared-memory accumulation is measured here: fewer than 65536 synapses
+// into any neuron and sum(|q| >> 16) + 1 over them below 2^31 - 2^20.
 static int finish_tables(g4s_net *n) {
   G4S_CUDA(launch_sort_rows(n->v, n->stream));
-  n->geo_ready = false;
+  n->team_ready = false;
   unsigned *cnt = nullptr;
   unsigned long long *mag = nullptr, *out = nullptr;
   cudaError_t e = cudaMalloc((void **)&cnt, (size_t)n->v.n * 4);
@@ -396,6 +470,114 @@ static int finish_tables(g4s_net *n) {
   return check_status(n, "row sort");
 }
 
+// Results of one chunk of `cs` steps: per-step counts, raster offsets and stamps, and the
+// raster itself when recorded; each step's ids sorted (the device order is by CTA).
+static int absorb_chunk(g4s_net *n, int cs, int64_t *spikes) {
+  NetView &v = n->v;
+  G4S_CUDA(cudaMemcpyAsync(n->h_counts, v.counts, (size_t)cs * 4, cudaMemcpyDeviceToHost, n->stream));
+  G4S_CUDA(cudaMemcpyAsync(n->h_base, v.base, (size_t)cs * 8, cudaMemcpyDeviceToHost, n->stream));
+  G4S_CUDA(cudaMemcpyAsync(n->h_stamps, v.stamps, (size_t)cs * 16, cudaMemcpyDeviceToHost, n->stream));
+  G4S_CUDA(cudaStreamSynchronize(n->stream));
+  const int64_t chunk_total = (int64_t)n->h_base[cs - 1] + n->h_counts[cs - 1];
+  if (n->desc.record_raster && chunk_total > 0) {
+    G4S_CUDA(cudaMemcpyAsync(n->h_raster, v.raster, (size_t)chunk_total * 4, cudaMemcpyDeviceToHost, n->stream));
+    G4S_CUDA(cudaStreamSynchronize(n->stream));
+    const size_t off = n->rt.size();
+    n->rt.resize(off + (size_t)chunk_total);
+    n->rid.resize(off + (size_t)chunk_total);
+    for (int lt = 0; lt < cs; ++lt) {
+      int *b = n->h_raster + n->h_base[lt];
+      std::sort(b, b + n->h_counts[lt]);
+      const int32_t t = (int32_t)(n->t_abs + lt);
+      for (int q = 0; q < n->h_counts[lt]; ++q) {
+        n->rt[off + (size_t)n->h_base[lt] + q] = t;
+        n->rid[off + (size_t)n->h_base[lt] + q] = b[q];
+      }
+    }
+  }
+  for (int lt = 0; lt < cs; ++lt) {
+    n->counts.push_back(n->h_counts[lt]);
+    const unsigned long long s0 = n->h_stamps[2 * lt], s1 = n->h_stamps[2 * lt + 1];
+    const unsigned long long s2 = lt + 1 < cs ? n->h_stamps[2 * lt + 2] : 0ull;
+    n->upd_ms.push_back(s1 > s0 ? (float)((s1 - s0) * 1e-6) : 0.0f);
+    n->step_ms.push_back(s2 > s0 ? (float)((s2 - s0) * 1e-6) : 0.0f);
+  }
+  *spikes = chunk_total;
+  n->t_abs += cs;
+  return G4S_OK;
+}
+
+// ---------------------------------------------------------------------------------------
+// One launch of the team kernel over several networks (a "round"): network i advances
+// steps[i] steps (at most its chunk length).  Multi-CTA teams are queued first, then the
+// one-CTA teams by decreasing work, so that long networks start early.
+// ---------------------------------------------------------------------------------------
+static int team_round(g4s_net *const *nets, const int *steps, const bool *last, int count, TeamLaunch &L,
+                      cudaStream_t s, unsigned long long limit_ns, int stall, double *kernel_ms, int64_t *launches) {
+  std::vector<int> order;
+  int nslots = 0, maxteam = 1;
+  size_t smem = 16;
+  for (int i = 0; i < count; ++i)
+    if (steps[i] > 0) {
+      order.push_back(i);
+      nslots += nets[i]->team_p;
+      maxteam = std::max(maxteam, nets[i]->team_p);
+      smem = std::max(smem, team_smem(nets[i]->team_rc));
+    }
+  if (order.empty()) return G4S_OK;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+    const g4s_net *x = nets[a], *y = nets[b];
+    if ((x->team_p > 1) != (y->team_p > 1)) return x->team_p > 1;
+    if (x->team_p != y->team_p) return x->team_p > y->team_p;
+    return (double)x->v.n * steps[a] * x->v.nsyn > (double)y->v.n * steps[b] * y->v.nsyn;
+  });
+  int rc = L.reserve(count, nslots);
+  if (rc) return rc;
+  int k = 0;
+  for (int i : order) {
+    g4s_net *n = nets[i];
+    TeamItem &it = L.h_items[i];
+    it.v = n->v;
+    it.seg = n->seg;
+    it.list = n->list;
+    it.t_abs0 = n->t_abs;
+    it.steps = steps[i];
+    it.last = last[i] ? 1 : 0;
+    it.team = n->team_p;
+    it.rc = (int)n->team_rc;
+    it.sync = n->gs;
+    for (int r = 0; r < n->team_p; ++r) L.h_slots[k++] = make_int2(i, r);
+    G4S_CUDA(cudaMemsetAsync(n->v.counts, 0, (size_t)steps[i] * sizeof(int), s));
+    G4S_CUDA(cudaMemsetAsync(n->v.stamps, 0, ((size_t)steps[i] * 2 + 2) * 8, s));
+    G4S_CUDA(cudaMemsetAsync(n->v.status, 0, sizeof(int), s));
+    G4S_CUDA(cudaMemsetAsync(n->gs, 0, sizeof(GridSync), s));
+  }
+  for (int i = 0; i < count; ++i)
+    if (steps[i] <= 0) L.h_items[i].steps = 0;
+  L.h_ctl[0] = nslots;
+  L.h_ctl[1] = 0;
+  G4S_CUDA(cudaMemcpyAsync(L.d_items, L.h_items, sizeof(TeamItem) * count, cudaMemcpyHostToDevice, s));
+  G4S_CUDA(cudaMemcpyAsync(L.d_slots, L.h_slots, sizeof(int2) * nslots, cudaMemcpyHostToDevice, s));
+  G4S_CUDA(cudaMemcpyAsync(L.d_ctl, L.h_ctl, 8, cudaMemcpyHostToDevice, s));
+  int gmax = 0;
+  G4S_CUDA(team_max_blocks(smem, &gmax));
+  if (gmax < maxteam) return set_error(G4S_ERR_CUDA, "team larger than the co-resident grid");
+  const int grid = std::min(nslots, gmax);
+  G4S_CUDA(cudaEventRecord(L.e0, s));
+  G4S_CUDA(launch_team(L.d_items, L.d_slots, L.d_ctl, L.d_ctl + 1, grid, smem, limit_ns, stall, s));
+  G4S_CUDA(cudaEventRecord(L.e1, s));
+  G4S_CUDA(cudaEventSynchronize(L.e1));
+  float ms = 0.0f;
+  G4S_CUDA(cudaEventElapsedTime(&ms, L.e0, L.e1));
+  *kernel_ms += ms;
+  *launches += 1;
+  for (int i : order) {
+    rc = check_status(nets[i], "team step kernel");
+    if (rc) return rc;
+  }
+  return G4S_OK;
+}
+
 static int run_net(g4s_net *n, int32_t steps, int32_t alg_in) {
   if (steps < 0) return set_error(G4S_ERR_INVALID, "steps must be >= 0");
   if (alg_in < 0 || alg_in > kAlgAuto) return set_error(G4S_ERR_INVALID, "unknown algorithm");
@@ -404,73 +586,51 @@ static int run_net(g4s_net *n, int32_t steps, int32_t alg_in) {
   NetView &v = n->v;
   if (n->shape.k_hint <= 0) n->shape.k_hint = (int)std::max<int64_t>(1, v.n / 20);
   if (alg == kAlgSKL) {
-    int rc0 = prepare_owner(n);
+    int rc0 = prepare_team(n);
     if (rc0) return rc0;
   }
-  const bool owner = alg == kAlgSKL && n->owner_ok && n->geo_ready;
+  const bool team = alg == kAlgSKL && n->team_ok && n->team_ready;
   const auto w0 = std::chrono::steady_clock::now();
   G4S_CUDA(cudaEventRecord(n->ev0, n->stream));
   int64_t remaining = steps, spikes = 0, launches = 0;
   double kernel_ms = 0.0;
   while (remaining > 0) {
-    const int cs = (int)std::min<int64_t>(remaining, n->chunk_steps);
+    const int cs = (int)std::min<int64_t>(remaining, team ? n->chunk_steps : n->chunk_legacy);
     const bool last_chunk = remaining == cs;
-    G4S_CUDA(cudaMemsetAsync(v.counts, 0, (size_t)cs * sizeof(int), n->stream));
-    G4S_CUDA(cudaMemsetAsync(v.stamps, 0, ((size_t)cs * 2 + 2) * 8, n->stream));
-    if (alg == kAlgSKL) G4S_CUDA(cudaMemsetAsync(n->gs, 0, sizeof(GridSync), n->stream));
-    G4S_CUDA(cudaEventRecord(n->ek0, n->stream));
-    if (owner) {
-      G4S_CUDA(launch_owner(v, n->geo, n->seg, n->t_abs, cs, last_chunk, n->gs, n->barrier_ns, n->barrier_stall,
-                            n->stream));
+    if (team) {
+      g4s_net *one[1] = {n};
+      int rc = team_round(one, &cs, &last_chunk, 1, n->launch, n->stream, n->barrier_ns, n->barrier_stall,
+                          &kernel_ms, &launches);
       n->barrier_stall = 0;
-      launches += 1;
-    } else if (alg == kAlgSKL) {
-      G4S_CUDA(launch_persistent(v, n->t_abs, cs, last_chunk, n->gs, n->barrier_ns, n->shape.group,
-                                 n->barrier_stall, n->stream));
-      n->barrier_stall = 0;
-      launches += 1;
+      if (rc) return rc;
     } else {
-      for (int lt = 0; lt < cs; ++lt) {
-        G4S_CUDA(launch_update(v, n->t_abs, lt, last_chunk && lt == cs - 1, n->stream));
-        G4S_CUDA(launch_deliver(v, lt, alg, n->shape, n->stream));
-      }
-      launches += 2 * (int64_t)cs;
-    }
-    G4S_CUDA(cudaEventRecord(n->ek1, n->stream));
-    G4S_CUDA(cudaMemcpyAsync(n->h_counts, v.counts, (size_t)cs * 4, cudaMemcpyDeviceToHost, n->stream));
-    G4S_CUDA(cudaMemcpyAsync(n->h_base, v.base, (size_t)cs * 8, cudaMemcpyDeviceToHost, n->stream));
-    G4S_CUDA(cudaMemcpyAsync(n->h_stamps, v.stamps, (size_t)cs * 16, cudaMemcpyDeviceToHost, n->stream));
-    int rc = check_status(n, alg == kAlgSKL ? "persistent step kernel" : "step kernels");
-    if (rc) return rc;
-    float kms = 0.0f;
-    G4S_CUDA(cudaEventElapsedTime(&kms, n->ek0, n->ek1));
-    kernel_ms += kms;
-    const int64_t chunk_total = (int64_t)n->h_base[cs - 1] + n->h_counts[cs - 1];
-    if (n->desc.record_raster && chunk_total > 0) {
-      G4S_CUDA(cudaMemcpyAsync(n->h_raster, v.raster, (size_t)chunk_total * 4, cudaMemcpyDeviceToHost, n->stream));
-      G4S_CUDA(cudaStreamSynchronize(n->stream));
-      const size_t off = n->rt.size();
-      n->rt.resize(off + (size_t)chunk_total);
-      n->rid.resize(off + (size_t)chunk_total);
-      for (int lt = 0; lt < cs; ++lt) {
-        int *b = n->h_raster + n->h_base[lt];
-        std::sort(b, b + n->h_counts[lt]);
-        const int32_t t = (int32_t)(n->t_abs + lt);
-        for (int q = 0; q < n->h_counts[lt]; ++q) {
-          n->rt[off + (size_t)n->h_base[lt] + q] = t;
-          n->rid[off + (size_t)n->h_base[lt] + q] = b[q];
+      G4S_CUDA(cudaMemsetAsync(v.counts, 0, (size_t)cs * sizeof(int), n->stream));
+      G4S_CUDA(cudaMemsetAsync(v.stamps, 0, ((size_t)cs * 2 + 2) * 8, n->stream));
+      if (alg == kAlgSKL) G4S_CUDA(cudaMemsetAsync(n->gs, 0, sizeof(GridSync), n->stream));
+      G4S_CUDA(cudaEventRecord(n->ek0, n->stream));
+      if (alg == kAlgSKL) {
+        G4S_CUDA(launch_persistent(v, n->t_abs, cs, last_chunk, n->gs, n->barrier_ns, n->shape.group,
+                                   n->barrier_stall, n->stream));
+        n->barrier_stall = 0;
+        launches += 1;
+      } else {
+        for (int lt = 0; lt < cs; ++lt) {
+          G4S_CUDA(launch_update(v, n->t_abs, lt, last_chunk && lt == cs - 1, n->stream));
+          G4S_CUDA(launch_deliver(v, lt, alg, n->shape, n->stream));
         }
+        launches += 2 * (int64_t)cs;
       }
+      G4S_CUDA(cudaEventRecord(n->ek1, n->stream));
+      int rc = check_status(n, alg == kAlgSKL ? "persistent step kernel" : "step kernels");
+      if (rc) return rc;
+      float kms = 0.0f;
+      G4S_CUDA(cudaEventElapsedTime(&kms, n->ek0, n->ek1));
+      kernel_ms += kms;
     }
-    for (int lt = 0; lt < cs; ++lt) {
-      n->counts.push_back(n->h_counts[lt]);
-      const unsigned long long s0 = n->h_stamps[2 * lt], s1 = n->h_stamps[2 * lt + 1];
-      const unsigned long long s2 = lt + 1 < cs ? n->h_stamps[2 * lt + 2] : 0ull;
-      n->upd_ms.push_back(s1 > s0 ? (float)((s1 - s0) * 1e-6) : 0.0f);
-      n->step_ms.push_back(s2 > s0 ? (float)((s2 - s0) * 1e-6) : 0.0f);
-    }
-    spikes += chunk_total;
-    n->t_abs += cs;
+    int64_t chunk_spikes = 0;
+    int rc = absorb_chunk(n, cs, &chunk_spikes);
+    if (rc) return rc;
+    spikes += chunk_spikes;
     remaining -= cs;
   }
   G4S_CUDA(cudaEventRecord(n->ev1, n->stream));
@@ -484,6 +644,65 @@ static int run_net(g4s_net *n, int32_t steps, int32_t alg_in) {
   n->last_alg = alg;
   n->last_kernel_ms = kernel_ms;
   n->last_launches = launches;
+  return G4S_OK;
+}
+
+// Several networks advanced together by the SKL team kernel: network i runs steps[i]
+// further steps; each round advances every unfinished network by up to its chunk length
+// in one persistent launch.
+static int run_nets(g4s_net *const *nets, const int32_t *steps, int count, double *dev_ms, int64_t *launches) {
+  if (count <= 0) return set_error(G4S_ERR_INVALID, "count must be > 0");
+  std::vector<int64_t> remaining(count);
+  for (int i = 0; i < count; ++i) {
+    if (!nets[i]) return set_error(G4S_ERR_INVALID, "null handle in batch");
+    if (steps[i] < 0 || nets[i]->t_abs + steps[i] > (int64_t)INT32_MAX)
+      return set_error(G4S_ERR_INVALID, "bad step count in batch");
+    for (int j = 0; j < i; ++j)
+      if (nets[j] == nets[i]) return set_error(G4S_ERR_INVALID, "a handle appears twice in the batch");
+    int rc = prepare_team(nets[i]);
+    if (rc) return rc;
+    if (!nets[i]->team_ok)
+      return set_error(G4S_ERR_INVALID, "a network of the batch does not fit the team kernel");
+    remaining[i] = steps[i];
+    nets[i]->last_spikes = 0;
+  }
+  static thread_local TeamLaunch L;
+  cudaStream_t s = nets[0]->stream;
+  std::vector<int> cs(count);
+  std::unique_ptr<bool[]> last(new bool[count]);
+  double kms = 0.0;
+  int64_t nl = 0;
+  const auto w0 = std::chrono::steady_clock::now();
+  for (;;) {
+    bool any = false;
+    for (int i = 0; i < count; ++i) {
+      cs[i] = (int)std::min<int64_t>(remaining[i], nets[i]->chunk_steps);
+      last[i] = cs[i] > 0 && cs[i] == remaining[i];
+      any = any || cs[i] > 0;
+    }
+    if (!any) break;
+    int rc = team_round(nets, cs.data(), last.get(), count, L, s, nets[0]->barrier_ns, 0, &kms, &nl);
+    if (rc) return rc;
+    for (int i = 0; i < count; ++i)
+      if (cs[i] > 0) {
+        int64_t sp = 0;
+        rc = absorb_chunk(nets[i], cs[i], &sp);
+        if (rc) return rc;
+        nets[i]->last_spikes += sp;
+        nets[i]->total_spikes += sp;
+        remaining[i] -= cs[i];
+      }
+  }
+  const double wall = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - w0).count();
+  for (int i = 0; i < count; ++i) {
+    nets[i]->last_alg = kAlgSKL;
+    nets[i]->last_kernel_ms = kms;
+    nets[i]->last_ms = wall;
+    nets[i]->last_wall_ms = wall;
+    nets[i]->last_launches = nl;
+  }
+  if (dev_ms) *dev_ms = kms;
+  if (launches) *launches = nl;
   return G4S_OK;
 }
 
@@ -636,19 +855,24 @@ int g4s_net_set_geometry(g4s_net *n, int32_t owner_blocks) {
   if (!n) return set_error(G4S_ERR_INVALID, "null handle");
   if (owner_blocks < 0) return set_error(G4S_ERR_INVALID, "owner_blocks must be >= 0 (0 = automatic)");
   n->want_p = owner_blocks;
-  n->geo_ready = false;
-  n->owner_ok = true;
+  n->team_ready = false;
+  n->team_ok = true;
   return G4S_OK;
 }
 
 int g4s_net_get_geometry(g4s_net *n, int32_t *owner_blocks, int64_t *slice) {
   if (!n) return set_error(G4S_ERR_INVALID, "null handle");
-  int rc = prepare_owner(n);
+  int rc = prepare_team(n);
   if (rc) return rc;
-  const bool ok = n->owner_ok && n->geo_ready;
-  if (owner_blocks) *owner_blocks = ok ? n->geo.p : 0;
-  if (slice) *slice = ok ? n->geo.rc : 0;
+  const bool ok = n->team_ok && n->team_ready;
+  if (owner_blocks) *owner_blocks = ok ? n->team_p : 0;
+  if (slice) *slice = ok ? n->team_rc : 0;
   return G4S_OK;
+}
+
+int g4s_nets_run(g4s_net **nets, const int32_t *steps, int32_t count, double *device_ms, int64_t *launches) {
+  if (!nets || !steps) return set_error(G4S_ERR_INVALID, "null argument");
+  return run_nets(nets, steps, count, device_ms, launches);
 }
 
 int g4s_net_reset(g4s_net *n) {

@@ -33,17 +33,17 @@ cudaError_t launch_persistent(const NetView &v, int64_t t_abs0, int nsteps, bool
 cudaError_t launch_stats(const NetView &v, double *out, cudaStream_t s);
 int persistent_blocks();
 
-// Owner-computes SKL (g4s_owner.cu).
+// SKL team kernel (g4s_team.cu).
 constexpr int kMaxSortedNsyn = 16384;          // rows are sorted in shared memory
-constexpr size_t kOwnerSmemLimit = 200 * 1024; // shared memory per CTA for currents + spikes
+constexpr size_t kTeamSmemLimit = 200 * 1024;  // shared memory per CTA for currents + spikes
 cudaError_t launch_sort_rows(const NetView &v, cudaStream_t s);
-cudaError_t launch_segoff(const NetView &v, const OwnerGeom &geo, uint16_t *seg, cudaStream_t s);
-cudaError_t launch_owner(const NetView &v, const OwnerGeom &geo, const uint16_t *seg, int64_t t_abs0, int nsteps,
-                         bool last_chunk, GridSync *gs, unsigned long long limit_ns, int stall, cudaStream_t s);
+cudaError_t launch_segoff(const NetView &v, int team, int64_t rc, uint16_t *seg, cudaStream_t s);
 cudaError_t launch_inbound(const NetView &v, unsigned *cnt, unsigned long long *mag, unsigned long long *out,
                            cudaStream_t s);
-cudaError_t owner_max_blocks(size_t smem, int *out);
-size_t owner_smem(int64_t rc);
+cudaError_t launch_team(const TeamItem *items, const int2 *slots, const int *nslots, int *slot_head, int grid,
+                        size_t smem, unsigned long long limit_ns, int stall, cudaStream_t s);
+cudaError_t team_max_blocks(size_t smem, int *out);
+size_t team_smem(int64_t rc);
 
 // Error reporting (thread-local message behind g4s_last_error()).
 int set_error(int code, const std::string &msg);

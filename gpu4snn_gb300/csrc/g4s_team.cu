@@ -1,0 +1,448 @@
+// g4s_team.cu — the SKL step loop as an owner-computes team kernel (the GB300 design of
+// SKL_deliverspks, gpu4snn.cu:669-716), for one network or many, plus the table
+// preparation it needs.
+//
+// Teams.  A launch runs a list of networks (TeamItem); network i is simulated by a team
+// of T_i CTAs.  The CTAs of the cooperative, persistent grid take (network, rank) slots
+// from one ordered queue; multi-CTA teams come first in the queue, so a team's members
+// start together.  A single network on the whole GPU is a one-item launch with a team of
+// one CTA per SM; a batched ensemble is a many-item launch where most networks fit one
+// CTA.
+//
+// Target ownership.  Team rank r owns the neurons [r Rc, (r+1) Rc) of its network and
+// keeps their synaptic currents in shared memory for the whole launch, as two 32-bit
+// words per neuron: the Q32.32 current q = A * 2^16 + B, with B the sum of the weights'
+// low 16 bits and A the sum of their high 48 bits.  Shared-memory 32-bit atomics are
+// about five times faster than 64-bit ones on this part, and the split is exact as long
+// as no neuron has 65536 or more incoming synapses and the sum of |q_i| / 2^16 + 1 over
+// its incoming synapses stays below 2^31; k_inbound checks both once per table (the
+// host falls back to the global-atomic persistent kernel otherwise).
+//
+// Per step, for each team:
+//   update    every rank updates its own neurons (current read from and cleared in shared
+//             memory) and collects its spikes in shared memory;
+//   exchange  one-CTA team: nothing, the spike list stays in shared memory.  Larger team:
+//             each rank appends its spikes to the network's global list of the step (two
+//             lists, by step parity), then a team barrier with a bounded spin;
+//   delivery  one-CTA team: whole spiking rows, 128-bit loads, flat over all threads.
+//             Larger team: every rank streams, for every spike, the segment of the
+//             spiking row whose targets fall in its slice (rows are sorted by target and
+//             a per-row offset table gives the segment): a warp takes 32 spikes, scans
+//             their segment lengths and walks the concatenated segments, eight synapses
+//             per lane in flight.  Each weight goes into the rank's own shared memory.
+//   The raster records the spike ids of every step while its buffer has room.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "g4s_device.cuh"
+#include "g4s_internal.h"
+
+namespace g4s {
+
+// ---------------------------------------------------------------------------------------
+// Row sort: every row's (target, weight) pairs in ascending target order, unused slots
+// (negative targets, i.e. huge as unsigned) last.  One CTA per row, bitonic network over
+// 64-bit keys (target << 32 | weight bits) in shared memory.
+// ---------------------------------------------------------------------------------------
+__global__ void k_sort_rows(NetView v, int p2) {
+  extern __shared__ unsigned long long s_key[];
+  for (int64_t row = blockIdx.x; row < v.n; row += gridDim.x) {
+    int *ri = const_cast<int *>(v.idx) + row * v.stride;
+    float *rw = const_cast<float *>(v.w) + row * v.stride;
+    for (int j = threadIdx.x; j < p2; j += blockDim.x)
+      s_key[j] = j < v.stride ? ((unsigned long long)(unsigned)ri[j] << 32) | __float_as_uint(rw[j])
+                              : 0xFFFFFFFFFFFFFFFFull;
+    __syncthreads();
+    for (int k = 2; k <= p2; k <<= 1)
+      for (int j = k >> 1; j > 0; j >>= 1) {
+        for (int i = threadIdx.x; i < p2; i += blockDim.x) {
+          const int l = i ^ j;
+          if (l > i) {
+            const unsigned long long a = s_key[i], b = s_key[l];
+            const bool up = (i & k) == 0;
+            if ((a > b) == up) {
+              s_key[i] = b;
+              s_key[l] = a;
+            }
+          }
+        }
+        __syncthreads();
+      }
+    for (int j = threadIdx.x; j < v.stride; j += blockDim.x) {
+      const unsigned long long x = s_key[j];
+      ri[j] = (int)(x >> 32);
+      rw[j] = __uint_as_float((unsigned)x);
+    }
+    __syncthreads();
+  }
+}
+
+// Segment table: seg[row][k] = first slot of the sorted row whose target is >= k*Rc, for
+// k = 0..T (unused slots compare as huge and lie beyond seg[row][T]).  One warp per row,
+// one binary search per boundary.
+__global__ void k_segoff(NetView v, int T, int64_t Rc, uint16_t *seg) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t row = warp; row < v.n; row += nwarps) {
+    const int *ri = v.idx + row * v.stride;
+    for (int k = lane; k <= T; k += 32) {
+      const int64_t bound = (int64_t)k * Rc;
+      int lo = 0, hi = v.stride;
+      while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if ((int64_t)(unsigned)ri[mid] < bound)
+          lo = mid + 1;
+        else
+          hi = mid;
+      }
+      seg[row * (T + 1) + k] = (uint16_t)lo;
+    }
+  }
+}
+
+// Exactness bound of the split accumulation: per target, the number of incoming synapses
+// and the sum of (|q| >> 16) + 1 over them; out[0] = max count, out[1] = max sum.
+__global__ void k_inbound(NetView v, unsigned *cnt, unsigned long long *mag) {
+  const int64_t total = v.n * (int64_t)v.stride;
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < total; g += (int64_t)gridDim.x * blockDim.x) {
+    const int t = v.idx[g];
+    if (t < 0) continue;
+    const long long q = wfix(v.w[g]);
+    const unsigned long long a = (unsigned long long)(q < 0 ? -q : q) >> 16;
+    atomicAdd(cnt + t, 1u);
+    atomicAdd(mag + t, a + 1ull);
+  }
+}
+
+__global__ void k_inbound_max(int64_t n, const unsigned *cnt, const unsigned long long *mag,
+                              unsigned long long *out) {
+  unsigned long long mc = 0, mm = 0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    mc = max(mc, (unsigned long long)cnt[i]);
+    mm = max(mm, mag[i]);
+  }
+  atomicMax(out, mc);
+  atomicMax(out + 1, mm);
+}
+
+// Split-accumulator add: A += q >> 16 (arithmetic), B += q & 0xFFFF.
+__device__ __forceinline__ void acc_add(unsigned base_a, unsigned base_b, unsigned off, long long q) {
+  asm volatile("red.shared.add.s32 [%0], %1;" ::"r"(base_a + off * 4u), "r"((int)(q >> 16)) : "memory");
+  asm volatile("red.shared.add.u32 [%0], %1;" ::"r"(base_b + off * 4u), "r"((unsigned)(q & 0xFFFF)) : "memory");
+}
+
+__device__ __forceinline__ void acc_add4(unsigned base_a, unsigned base_b, int lo, const int4 t, const float4 w) {
+  if (t.x >= 0) acc_add(base_a, base_b, (unsigned)(t.x - lo), wfix(w.x));
+  if (t.y >= 0) acc_add(base_a, base_b, (unsigned)(t.y - lo), wfix(w.y));
+  if (t.z >= 0) acc_add(base_a, base_b, (unsigned)(t.z - lo), wfix(w.z));
+  if (t.w >= 0) acc_add(base_a, base_b, (unsigned)(t.w - lo), wfix(w.w));
+}
+
+// ---------------------------------------------------------------------------------------
+// One team member's share of one network for the steps of this launch.
+// ---------------------------------------------------------------------------------------
+template <int NT>
+__device__ void team_run(const TeamItem &it, int rank, unsigned char *s_raw, int *s_nspk, long long *s_gpos,
+                         unsigned long long limit_ns, int stall) {
+  const NetView &v = it.v;
+  const int T = it.team, rc = it.rc;
+  int *s_a = reinterpret_cast<int *>(s_raw);
+  unsigned *s_b = reinterpret_cast<unsigned *>(s_raw + (size_t)rc * 4);
+  int *s_spk = reinterpret_cast<int *>(s_raw + (size_t)rc * 8);
+  const int64_t lo = min((int64_t)rank * rc, v.n);
+  const int64_t hi = min(lo + rc, v.n);
+  const int cnt = (int)(hi - lo);
+  const unsigned base_a = (unsigned)__cvta_generic_to_shared(s_a);
+  const unsigned base_b = (unsigned)__cvta_generic_to_shared(s_b);
+  const unsigned segw = (unsigned)T + 1;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  constexpr int kWarps = NT / 32;
+  const bool shared_list = T == 1 && stall == 0;  // the whole network in this CTA
+  const unsigned nb = (unsigned)T + (unsigned)stall;  // stall > 0 only under fault injection
+  const bool lead = rank == 0 && threadIdx.x == 0;
+
+  for (int i = threadIdx.x; i < cnt; i += NT) {
+    const long long q = __ldcg(v.acc + lo + i);
+    s_a[i] = (int)(q >> 16);
+    s_b[i] = (unsigned)(q & 0xFFFF);
+  }
+  if (threadIdx.x == 0) *s_nspk = 0;
+  __syncthreads();
+
+  unsigned epoch = 0;
+  long long base = 0;
+  for (int lt = 0; lt < it.steps; ++lt) {
+    const int64_t t_abs = it.t_abs0 + lt;
+    const bool last = it.last && lt == it.steps - 1;
+    if (lead) {
+      v.base[lt] = base;
+      if (v.stamps) v.stamps[2 * lt] = globaltimer();
+    }
+    // ---- update of the owned neurons, two per thread per round with the loads first
+    for (int i0 = threadIdx.x; i0 < cnt; i0 += 2 * NT) {
+      const int i1 = i0 + NT;
+      const bool h1 = i1 < cnt;
+      const int64_t n0 = lo + i0, n1 = lo + (h1 ? i1 : i0);
+      float2 s0 = v.vu[n0], s1 = v.vu[n1];
+      const float4 p0 = v.abcd[n0], p1 = v.abcd[n1];
+      const long long a0 = (long long)s_a[i0] * 65536 + s_b[i0];
+      const long long a1 = h1 ? (long long)s_a[i1] * 65536 + s_b[i1] : 0;
+      s_a[i0] = 0;
+      s_b[i0] = 0;
+      if (h1) {
+        s_a[i1] = 0;
+        s_b[i1] = 0;
+      }
+      const float z0 = normal(v.seed, (uint64_t)n0, (uint64_t)t_abs);
+      const float z1 = normal(v.seed, (uint64_t)n1, (uint64_t)t_abs);
+      float I0, I1;
+      const bool k0 = izh_step(s0.x, s0.y, I0, p0, n0 < v.nexc ? v.ge : v.gi, z0, a0);
+      const bool k1 = izh_step(s1.x, s1.y, I1, p1, n1 < v.nexc ? v.ge : v.gi, z1, a1) && h1;
+      v.vu[n0] = s0;
+      if (h1) v.vu[n1] = s1;
+      if (last) {
+        v.ilast[n0] = I0;
+        if (h1) v.ilast[n1] = I1;
+      }
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const bool spk = h ? k1 : k0;
+        if (!spk) continue;
+        const int64_t n = h ? n1 : n0;
+        SpikeStat st = v.sstat[n];
+        st.nospks += 1;
+        if (st.last >= 0) {
+          const long long isi = t_abs - st.last;
+          st.nisi += 1;
+          st.s1 += isi;
+          st.s2 += isi * isi;
+        }
+        st.last = (int)t_abs;
+        v.sstat[n] = st;
+        s_spk[atomicAdd(s_nspk, 1)] = (int)n;
+      }
+    }
+    __syncthreads();
+    const int nspk = *s_nspk;
+    if (threadIdx.x == 0) *s_gpos = shared_list ? 0 : (nspk ? atomicAdd(v.counts + lt, nspk) : 0);
+    __syncthreads();
+    if (threadIdx.x == 0) *s_nspk = 0;
+    int *glist = it.list + (size_t)(lt & 1) * (size_t)v.n;
+    for (int j = threadIdx.x; j < nspk; j += NT) {
+      const int id = s_spk[j];
+      const long long pos = base + *s_gpos + j;
+      if (!shared_list) glist[*s_gpos + j] = id;
+      if (pos < v.raster_cap) v.raster[pos] = id;
+    }
+    int K = nspk;
+    if (shared_list) {
+      if (threadIdx.x == 0) v.counts[lt] = nspk;
+    } else {
+      // ---- the step's spike list is complete for the whole team after this barrier
+      if (!grid_barrier(it.sync, nb, epoch, epoch == 0 ? limit_ns * 16 : limit_ns)) return;
+      K = __ldcg(v.counts + lt);
+    }
+    if (lead && v.stamps) v.stamps[2 * lt + 1] = globaltimer();
+    if (shared_list) {
+      // ---- delivery, one-CTA team: flat over K whole rows of stride/4 vectors
+      const int rv = v.stride >> 2;
+      const int total = K * rv;
+      const int dq = NT / rv, dj = NT - dq * rv;
+      int q = threadIdx.x / rv, j = threadIdx.x - q * rv;
+      const int4 *ti = reinterpret_cast<const int4 *>(v.idx);
+      const float4 *wi = reinterpret_cast<const float4 *>(v.w);
+      const uint64_t pol = policy_evict_first();
+      for (int g = threadIdx.x; g < total; g += 2 * NT) {
+        const size_t o0 = (size_t)s_spk[q] * rv + j;
+        int q1 = q + dq, j1 = j + dj;
+        if (j1 >= rv) {
+          j1 -= rv;
+          q1 += 1;
+        }
+        const bool h1 = g + NT < total;
+        const size_t o1 = h1 ? (size_t)s_spk[q1] * rv + j1 : o0;
+        const int4 t0 = ld_stream_i4(ti + o0, pol), t1 = ld_stream_i4(ti + o1, pol);
+        const float4 w0 = ld_stream_f4(wi + o0, pol), w1 = ld_stream_f4(wi + o1, pol);
+        acc_add4(base_a, base_b, 0, t0, w0);
+        if (h1) acc_add4(base_a, base_b, 0, t1, w1);
+        q = q1 + dq;
+        j = j1 + dj;
+        if (j >= rv) {
+          j -= rv;
+          q += 1;
+        }
+      }
+    } else {
+      // ---- delivery, larger team: this rank's segment of every spiking row.  Spikes go
+      // to warps in batches of 32; when there are fewer batches than warps, `wpb` warps
+      // share a batch and split its run.  The next batch's spike ids and segment bounds
+      // are loaded before the current run is walked.
+      const int nbatch = (K + 31) >> 5;
+      const int wpb = nbatch >= kWarps ? 1 : kWarps / max(nbatch, 1);
+      const int groups = kWarps / wpb, gw = warp / wpb, wi = warp % wpb;
+      int s = 0, b = 0, len = 0;
+      auto fetch = [&](int batch) {
+        const int q = batch * 32 + lane;
+        s = 0;
+        b = 0;
+        len = 0;
+        if (gw < groups && batch < nbatch && q < K) {
+          s = __ldcg(glist + q);
+          const uint16_t *so = it.seg + (size_t)s * segw + rank;
+          b = so[0];
+          len = (int)so[1] - b;
+        }
+      };
+      fetch(gw);
+      for (int batch = gw; gw < groups && batch < nbatch; batch += groups) {
+        int incl = len;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+          if (lane >= o) incl += y;
+        }
+        const int total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+        const int excl = incl - len;
+        const long long rowoff = (long long)s * v.stride + b - excl;  // synapse f of the run: rowoff_j + f
+        fetch(batch + groups);                                        // next batch, in flight meanwhile
+        for (int f0 = wi * 256; f0 < total; f0 += wpb * 256) {
+          int t[8];
+          float w[8];
+#pragma unroll
+          for (int u = 0; u < 8; ++u) {
+            const int f = f0 + u * 32 + lane;
+            // spike j of the run holding f: last lane whose exclusive prefix is <= f
+            int jj = 0;
+#pragma unroll
+            for (int step = 16; step; step >>= 1) {
+              const int e = __shfl_sync(0xFFFFFFFFu, excl, jj + step);
+              if (e <= f) jj += step;
+            }
+            const long long off = __shfl_sync(0xFFFFFFFFu, rowoff, jj) + f;
+            t[u] = -1;
+            w[u] = 0.0f;
+            if (f < total) {
+              t[u] = __ldg(v.idx + off);
+              w[u] = __ldg(v.w + off);
+            }
+          }
+#pragma unroll
+          for (int u = 0; u < 8; ++u)
+            if (t[u] >= 0) acc_add(base_a, base_b, (unsigned)(t[u] - (int)lo), wfix(w[u]));
+        }
+      }
+    }
+    __syncthreads();
+    base += K;
+  }
+  // pending currents (from the last delivery) back to global memory for the next launch
+  for (int i = threadIdx.x; i < cnt; i += NT) v.acc[lo + i] = (long long)s_a[i] * 65536 + s_b[i];
+  __syncthreads();
+}
+
+// The persistent grid: CTAs take (network, rank) slots until the queue is empty.
+template <int NT>
+__global__ void __launch_bounds__(NT, 1) k_team(const TeamItem *__restrict__ items, const int2 *__restrict__ slots,
+                                                const int *nslots, int *slot_head, unsigned long long limit_ns,
+                                                int stall) {
+  extern __shared__ __align__(16) unsigned char s_raw[];
+  __shared__ int s_slot;
+  __shared__ int s_nspk;
+  __shared__ long long s_gpos;
+  const int ns = *nslots;
+  for (;;) {
+    if (threadIdx.x == 0) s_slot = atomicAdd(slot_head, 1);
+    __syncthreads();
+    const int sl = s_slot;
+    __syncthreads();
+    if (sl >= ns) break;
+    const int2 x = slots[sl];
+    const TeamItem &it = items[x.x];
+    if (it.steps > 0) team_run<NT>(it, x.y, s_raw, &s_nspk, &s_gpos, limit_ns, stall);
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+// Launchers.
+// ---------------------------------------------------------------------------------------
+constexpr int kTeamNT = 1024;
+
+size_t team_smem(int64_t rc) { return (size_t)rc * 12 + 16; }
+
+cudaError_t team_max_blocks(size_t smem, int *out) {
+  cudaError_t e = cudaFuncSetAttribute(k_team<kTeamNT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  int occ = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_team<kTeamNT>, kTeamNT, smem);
+  if (e != cudaSuccess) return e;
+  int dev = 0, sms = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  *out = occ * sms;
+  return cudaSuccess;
+}
+
+cudaError_t launch_team(const TeamItem *items, const int2 *slots, const int *nslots, int *slot_head, int grid,
+                        size_t smem, unsigned long long limit_ns, int stall, cudaStream_t s) {
+  cudaError_t e = cudaFuncSetAttribute(k_team<kTeamNT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3(kTeamNT);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k_team<kTeamNT>, items, slots, nslots, slot_head, limit_ns, stall);
+}
+
+cudaError_t launch_sort_rows(const NetView &v, cudaStream_t s) {
+  int p2 = 32;
+  while (p2 < v.stride) p2 <<= 1;
+  const size_t smem = (size_t)p2 * 8;
+  if (smem > 200 * 1024) return cudaErrorInvalidValue;
+  cudaError_t e = cudaFuncSetAttribute(k_sort_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  const int nt = p2 >= 4096 ? 1024 : (p2 >= 1024 ? 256 : 128);
+  int occ = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_sort_rows, nt, smem);
+  if (occ < 1) occ = 1;
+  int dev = 0, sms = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  int64_t g = (int64_t)sms * occ;
+  if (g > v.n) g = v.n;
+  k_sort_rows<<<(unsigned)g, nt, smem, s>>>(v, p2);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_segoff(const NetView &v, int team, int64_t rc, uint16_t *seg, cudaStream_t s) {
+  int dev = 0, sms = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  int64_t blocks = (v.n + 7) / 8;
+  if (blocks > (int64_t)sms * 16) blocks = (int64_t)sms * 16;
+  k_segoff<<<(unsigned)blocks, 256, 0, s>>>(v, team, rc, seg);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_inbound(const NetView &v, unsigned *cnt, unsigned long long *mag, unsigned long long *out,
+                           cudaStream_t s) {
+  int dev = 0, sms = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaError_t e = cudaMemsetAsync(cnt, 0, (size_t)v.n * 4, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(mag, 0, (size_t)v.n * 8, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(out, 0, 16, s);
+  if (e != cudaSuccess) return e;
+  k_inbound<<<(unsigned)(sms * 8), 512, 0, s>>>(v, cnt, mag);
+  k_inbound_max<<<(unsigned)(sms * 2), 512, 0, s>>>(v.n, cnt, mag, out);
+  return cudaGetLastError();
+}
+
+}  // namespace g4s

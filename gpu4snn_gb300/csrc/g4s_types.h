@@ -56,12 +56,18 @@ struct NetView {
   int *status;      // device error word (kErr*Code)
 };
 
-// Launch geometry of the owner-computes SKL kernel: p CTAs, CTA k owns the neurons
-// [k rc, (k+1) rc).
-struct OwnerGeom {
-  int p;       // owner CTAs
-  int pad;
-  int64_t rc;  // neurons per CTA slice
+// One network of a team-kernel launch: its arrays, the steps of this launch, and its
+// team (CTAs `team`, each owning `rc` neurons).
+struct TeamItem {
+  NetView v;
+  const uint16_t *seg;  // [n][team+1] row segment offsets (team > 1)
+  int *list;            // [2][n] spike lists of the step, by step parity (team > 1)
+  int64_t t_abs0;       // absolute step of the first step of this launch
+  int steps;            // steps of this launch (0: nothing to do)
+  int last;             // this launch ends the run: record the input current at its last step
+  int team;             // CTAs of the team
+  int rc;               // neurons per CTA slice
+  GridSync *sync;       // team barrier and error word
 };
 
 }  // namespace g4s

@@ -156,6 +156,18 @@ class Network:
         check(load().g4s_net_write_results(self._h, directory.encode(), None, elapsed_ms, elapsed_with_data_ms))
 
 
+def run_batch(nets: list[Network], steps) -> tuple[float, int]:
+    """Advance several networks together in shared persistent launches of the SKL team
+    kernel; network i runs steps[i] further steps.  Returns (device ms, launches)."""
+    if isinstance(steps, int):
+        steps = [steps] * len(nets)
+    handles = (C.c_void_p * len(nets))(*[n._h.value for n in nets])
+    st = np.ascontiguousarray(steps, dtype=np.int32)
+    ms, nl = C.c_double(), C.c_int64()
+    check(load().g4s_nets_run(C.cast(handles, C.c_void_p), ptr(st), len(nets), C.byref(ms), C.byref(nl)))
+    return ms.value, nl.value
+
+
 def conn_glibc(seed: int, n: int, nsyn: int, stride: int | None = None) -> tuple[np.ndarray, np.ndarray]:
     """The reference's host tables (glibc rand after srand(seed), gpu4snn.cu:873-898)."""
     stride = row_stride(nsyn) if stride is None else stride
@@ -171,4 +183,4 @@ def run_protocol(n: int, nsyn: int, iterations: int, algorithm: int = -1, mode: 
     check(load().g4s_run_protocol(n, nsyn, iterations, algorithm, mode, seed, conn_law, results_root.encode()))
 
 
-__all__ = ["Network", "Stats", "conn_glibc", "run_protocol", "row_stride", "CONN_GLIBC", "CONN_PHILOX"]
+__all__ = ["Network", "Stats", "conn_glibc", "run_batch", "run_protocol", "row_stride", "CONN_GLIBC", "CONN_PHILOX"]

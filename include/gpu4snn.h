@@ -126,6 +126,14 @@ int g4s_net_set_barrier_timeout(g4s_net *net, uint64_t ns);
  * kernel runs instead) and the neurons per CTA. */
 int g4s_net_set_geometry(g4s_net *net, int32_t owner_blocks);
 int g4s_net_get_geometry(g4s_net *net, int32_t *owner_blocks, int64_t *slice);
+
+/* Batched execution (the reference runs one network per launch sequence; this has no
+ * counterpart there beyond SKL_deliverspks, gpu4snn.cu:669-716): `count` independent
+ * handles, network i advancing steps[i] further steps, all in shared persistent launches
+ * of the SKL team kernel (a network that fits one CTA's shared memory runs on one CTA).
+ * Results land in each handle as after g4s_net_run.  *device_ms receives the CUDA-event
+ * time of the launches, *launches their number (either pointer may be NULL). */
+int g4s_nets_run(g4s_net **nets, const int32_t *steps, int32_t count, double *device_ms, int64_t *launches);
 int g4s_net_destroy(g4s_net *net);
 
 /* Host-side fault injection for failure-detection tests (nothing faults the GPU):

@@ -199,3 +199,24 @@ def test_owner_large_network(g4s, oracle):
         net.run(200, 4)
         assert np.array_equal(np.stack(net.raster()), np.stack(sim.raster()))
         compare_state(net, sim)
+
+
+def test_batch_matches_individual_runs(g4s, oracle):
+    """Networks of uneven size, fan-out, seed and drive advanced together by the team
+    kernel give exactly the results of each run alone (and of the oracle)."""
+    specs = [(1500, 100, 31, 0.8, 120), (4000, 800, 32, 1.2, 90), (20011, 300, 33, 1.0, 60),
+             (700, 699, 34, 2.0, 150), (3001, 37, 35, 0.5, 110)]
+    nets = [g4s.Network(n, s, seed=sd, drive_scale=dr, raster_budget_bytes=4 * n * 64) for n, s, sd, dr, _ in specs]
+    g4s.run_batch(nets, [st for *_, st in specs])
+    for net, (n, nsyn, seed, drive, steps) in zip(nets, specs):
+        d = oracle.make_desc(n, nsyn, seed, drive_scale=drive)
+        idx, w = oracle.conn_philox(d)
+        sim = oracle.Sim(d, idx, w)
+        sim.run(steps, threads=8)
+        assert net.info().steps_done == steps
+        assert np.array_equal(np.stack(net.raster()), np.stack(sim.raster())), (n, nsyn)
+        compare_state(net, sim)
+        with g4s.Network(n, nsyn, seed=seed, drive_scale=drive) as alone:
+            alone.run(steps, 4)
+            assert np.array_equal(np.stack(alone.raster()), np.stack(net.raster()))
+        net.close()
