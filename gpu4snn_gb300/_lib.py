@@ -100,6 +100,7 @@ SIGNATURES = [
     ("g4s_run_protocol", C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_uint64,
                                    C.c_int32, C.c_char_p]),
     ("g4s_conn_glibc", C.c_int, [C.c_uint32, C.c_int32, C.c_int32, C.c_int32, _P, _P]),
+    ("g4s_run_noalloc", C.c_int, [_P, C.c_int64, C.c_int32, C.c_int32, C.c_int32, _P, _P, _P, C.c_int64, _P, _P]),
     ("g4s_pinned_alloc", C.c_int, [C.c_uint64, C.POINTER(_P)]),
     ("g4s_pinned_free", C.c_int, [_P]),
 ]

@@ -1,0 +1,158 @@
+// g4s_noalloc.cu — g4s_run_noalloc: the SKL team kernel on caller-owned device arrays,
+// without any allocation.
+//
+// Some callers cannot call cudaMalloc while they step a network: code running inside a
+// stream capture of someone else's CUDA graph (allocation calls are not capturable),
+// real-time loops that must not pay the device-wide synchronisation an allocation may
+// imply, and hosts whose device memory is owned by a capped pool that this library cannot
+// draw from.  For them this entry point uses only memory it already has: the caller
+// passes the network's arrays and the output buffers, and the kernel's scratch (per-step
+// spike lists, the per-row segment table of a multi-CTA team, the team barrier and the
+// work-queue words) lives in one file-scope __device__ array of fixed size, which every
+// GPU that loads the library holds until the process exits.
+//
+// Limits: at most kNoAllocMaxNeurons neurons and kNoAllocMaxTeam CTAs, and at most 16384
+// neurons per CTA (the shared-memory slice of the team kernel).  Every call shares the
+// scratch array and leaves its contents behind; calls that overlap on the GPU (on
+// different streams, or without ordering between them) race on it and must not be made.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "../../include/gpu4snn.h"
+#include "g4s_internal.h"
+
+using namespace g4s;
+
+namespace {
+
+constexpr int64_t kNoAllocMaxNeurons = 131072;
+constexpr int kNoAllocMaxTeam = 8;
+constexpr int64_t kNoAllocMaxSlice = 16384;
+
+// Layout of the scratch array.
+constexpr size_t kOffSync = 0;                                  // GridSync (128 B)
+constexpr size_t kOffCtl = 128;                                 // int[4]: slot count, queue head, status
+constexpr size_t kOffSlots = 256;                               // int2[kNoAllocMaxTeam]
+constexpr size_t kOffItem = 512;                                // TeamItem
+constexpr size_t kOffList = 4096;                               // int[2][kNoAllocMaxNeurons]
+constexpr size_t kOffSeg = kOffList + 2 * kNoAllocMaxNeurons * 4;  // u16[kNoAllocMaxNeurons][kNoAllocMaxTeam + 1]
+constexpr size_t kScratchBytes = kOffSeg + (size_t)kNoAllocMaxNeurons * (kNoAllocMaxTeam + 1) * 2;
+
+static_assert(sizeof(GridSync) <= kOffCtl - kOffSync, "barrier word");
+static_assert(sizeof(int2) * kNoAllocMaxTeam <= kOffItem - kOffSlots, "slots");
+static_assert(sizeof(TeamItem) <= kOffList - kOffItem, "item");
+
+}  // namespace
+
+// The scratch of g4s_run_noalloc (about 3.4 MB per GPU, held until exit).
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
+
+// In host code g_noalloc_scratch names a host-side stand-in, not device memory: its
+// device address is looked up once per device, with that device current, and cached.
+static std::mutex g_scratch_mu;
+static void *g_scratch_dev[256];
+
+static int scratch_address(unsigned char **out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_error(e, "cudaGetDevice");
+  if (dev < 0 || dev >= 256) return set_error(G4S_ERR_CUDA, "device index out of range");
+  std::lock_guard<std::mutex> lock(g_scratch_mu);
+  if (!g_scratch_dev[dev]) {
+    void *p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) return cuda_error(e, "cudaGetSymbolAddress of the no-alloc scratch");
+    g_scratch_dev[dev] = p;
+  }
+  *out = static_cast<unsigned char *>(g_scratch_dev[dev]);
+  return G4S_OK;
+}
+
+extern "C" int g4s_run_noalloc(const g4s_dev_net *d, int64_t t_abs0, int32_t steps, int32_t team, int32_t last,
+                               int32_t *d_counts, int64_t *d_base, int32_t *d_raster, int64_t raster_cap,
+                               int32_t *d_status, void *stream) {
+  if (!d) return set_error(G4S_ERR_INVALID, "null network");
+  if (d->n < 2 || d->n > kNoAllocMaxNeurons)
+    return set_error(G4S_ERR_INVALID, "g4s_run_noalloc: n must be in [2, " + std::to_string(kNoAllocMaxNeurons) +
+                                          "], got " + std::to_string(d->n));
+  if (team < 1 || team > kNoAllocMaxTeam)
+    return set_error(G4S_ERR_INVALID, "g4s_run_noalloc: team must be in [1, " + std::to_string(kNoAllocMaxTeam) +
+                                          "], got " + std::to_string(team));
+  const int64_t rc = (d->n + team - 1) / team;
+  if (rc > kNoAllocMaxSlice)
+    return set_error(G4S_ERR_INVALID, "g4s_run_noalloc: more than " + std::to_string(kNoAllocMaxSlice) +
+                                          " neurons per CTA; use a larger team");
+  if (d->nsyn < 1 || d->stride < d->nsyn || d->stride % 4 != 0 || d->stride > kMaxSortedNsyn)
+    return set_error(G4S_ERR_INVALID, "g4s_run_noalloc: need 1 <= nsyn <= stride <= 16384, stride % 4 == 0");
+  if (d->nexc < 0 || d->nexc > d->n) return set_error(G4S_ERR_INVALID, "g4s_run_noalloc: bad nexc");
+  if (steps < 0 || t_abs0 < 0 || t_abs0 + steps > (int64_t)INT32_MAX)
+    return set_error(G4S_ERR_INVALID, "g4s_run_noalloc: bad step range");
+  if (!d->vu || !d->abcd || !d->acc || !d->i_last || !d->spike_stat || !d->idx || !d->w)
+    return set_error(G4S_ERR_INVALID, "g4s_run_noalloc: null network array");
+  if (steps > 0 && (!d_counts || !d_base)) return set_error(G4S_ERR_INVALID, "g4s_run_noalloc: null counts/base");
+  if (raster_cap < 0 || (raster_cap > 0 && !d_raster))
+    return set_error(G4S_ERR_INVALID, "g4s_run_noalloc: bad raster buffer");
+  if (steps == 0) return G4S_OK;
+
+  unsigned char *scr = nullptr;
+  int rc0 = scratch_address(&scr);
+  if (rc0) return rc0;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  GridSync *sync = reinterpret_cast<GridSync *>(scr + kOffSync);
+  int *ctl = reinterpret_cast<int *>(scr + kOffCtl);
+  int2 *slots = reinterpret_cast<int2 *>(scr + kOffSlots);
+  TeamItem *item = reinterpret_cast<TeamItem *>(scr + kOffItem);
+  int *list = reinterpret_cast<int *>(scr + kOffList);
+  uint16_t *seg = reinterpret_cast<uint16_t *>(scr + kOffSeg);
+
+  TeamItem h{};
+  NetView &v = h.v;
+  v.n = d->n;
+  v.nexc = d->nexc;
+  v.nsyn = d->nsyn;
+  v.stride = d->stride;
+  v.seed = d->seed;
+  v.ge = d->ge;
+  v.gi = d->gi;
+  v.vu = static_cast<float2 *>(d->vu);
+  v.abcd = static_cast<float4 *>(d->abcd);
+  v.acc = reinterpret_cast<long long *>(d->acc);
+  v.ilast = d->i_last;
+  v.sstat = static_cast<SpikeStat *>(d->spike_stat);
+  v.idx = d->idx;
+  v.w = d->w;
+  v.raster = d_raster;
+  v.raster_cap = raster_cap;
+  v.counts = d_counts;
+  v.base = reinterpret_cast<long long *>(d_base);
+  v.stamps = nullptr;
+  v.status = ctl + 2;
+  h.seg = seg;
+  h.list = list;
+  h.t_abs0 = t_abs0;
+  h.steps = steps;
+  h.last = last ? 1 : 0;
+  h.team = team;
+  h.rc = (int)rc;
+  h.sync = sync;
+  int2 hs[kNoAllocMaxTeam];
+  for (int r = 0; r < team; ++r) hs[r] = make_int2(0, r);
+  const int hc[2] = {team, 0};
+
+  // Everything that must start at zero: barrier and error word, queue head, step counts.
+  cudaError_t e = cudaMemsetAsync(scr, 0, kOffSlots, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d_counts, 0, (size_t)steps * sizeof(int32_t), s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(ctl, hc, sizeof hc, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(slots, hs, sizeof(int2) * team, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(item, &h, sizeof h, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess && team > 1) e = launch_segoff(v, team, rc, seg, s);
+  if (e == cudaSuccess)
+    e = launch_team(item, slots, ctl, ctl + 1, team, team_smem(rc), 2000000000ull, 0, s);
+  if (e == cudaSuccess && d_status) e = cudaMemcpyAsync(d_status, &sync->error, sizeof(int32_t), cudaMemcpyDeviceToDevice, s);
+  if (e != cudaSuccess) return cuda_error(e, "g4s_run_noalloc launch");
+  return G4S_OK;
+}

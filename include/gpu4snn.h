@@ -158,6 +158,44 @@ int g4s_net_write_results(g4s_net *net, const char *dir, const float *init_state
 int g4s_run_protocol(int32_t n, int32_t nsyn, int32_t iterations, int32_t algorithm, int32_t mode, uint64_t seed,
                      int32_t conn_law, const char *results_root);
 
+/* Device arrays of one network, owned by the caller (layouts as the library's own). */
+typedef struct g4s_dev_net {
+  int64_t n;          /* neurons                                                        */
+  int64_t nexc;       /* excitatory neurons: ids [0, nexc)                                */
+  int32_t nsyn;       /* synapses per neuron                                              */
+  int32_t stride;     /* row stride of the tables: a multiple of 4, nsyn <= stride <= 16384 */
+  uint64_t seed;      /* seed of the thalamic drive                                       */
+  float ge, gi;       /* thalamic gains of excitatory / inhibitory neurons                 */
+  void *vu;           /* float2[n]: v, u                                                   */
+  void *abcd;         /* float4[n]: a, b, c, d                                             */
+  int64_t *acc;       /* int64[n]: pending Q32.32 synaptic currents                        */
+  float *i_last;      /* float[n]: input current of the last step of a run                 */
+  void *spike_stat;   /* 32-byte records [n]: int32 nospks, last (-1 before the first
+                         spike), nisi, pad; int64 sum of intervals, sum of squares          */
+  const int32_t *idx; /* [n][stride] targets, every row ascending, unused slots (-1) last
+                         (as g4s_net_tables returns them)                                   */
+  const float *w;     /* [n][stride] weights                                                */
+} g4s_dev_net;
+
+/* The SKL team kernel on caller-owned device arrays, allocating nothing.  No counterpart
+ * in the reference.  For callers that cannot allocate device memory while they step a
+ * network: code inside a stream capture of another library's CUDA graph, real-time loops
+ * that cannot take an allocation's device-wide synchronisation, hosts whose device memory
+ * is a capped pool this library cannot draw from.  Advances `steps` steps from absolute
+ * step t_abs0 with a team of `team` CTAs (1..8); outputs, all device memory of the caller:
+ * d_counts int32[steps] spikes per step, d_base int64[steps] raster offset of each step,
+ * d_raster int32[raster_cap] spike ids (ids that do not fit are not recorded), d_status
+ * (may be NULL) 0 or a device error code; `last` = 1 records i_last at the last step.
+ * Stream-ordered on `stream` (NULL: the default stream).  The kernel's scratch is one
+ * fixed __device__ array of about 3.4 MB (held by every GPU that loads the library): at
+ * most 131072 neurons and 16384 neurons per CTA; larger requests are rejected with
+ * G4S_ERR_INVALID.  The first call on a device looks the array's address up, so make it
+ * before any stream capture.  All calls share the array: calls that overlap on the GPU
+ * race and must not be made. */
+int g4s_run_noalloc(const g4s_dev_net *net, int64_t t_abs0, int32_t steps, int32_t team, int32_t last,
+                    int32_t *d_counts, int64_t *d_base, int32_t *d_raster, int64_t raster_cap, int32_t *d_status,
+                    void *stream);
+
 /* Page-locked host buffers for fast table uploads and raster downloads (the reference
  * copies from pageable malloc memory, gpu4snn.cu:863-866, 910-911). */
 int g4s_pinned_alloc(uint64_t bytes, void **out);
