@@ -71,6 +71,23 @@ class NetInfo(C.Structure):
     ]
 
 
+class Request(C.Structure):
+    _fields_ = [("n", C.c_int64), ("nsyn", C.c_int32), ("steps", C.c_int32), ("seed", C.c_uint64),
+                ("drive_scale", C.c_float), ("record_raster", C.c_int32)]
+
+
+class RequestResult(C.Structure):
+    _fields_ = [("id", C.c_int64), ("status", C.c_int32), ("steps_done", C.c_int32), ("total_spikes", C.c_int64),
+                ("latency_ms", C.c_double), ("queue_ms", C.c_double), ("rate_hz", C.c_double),
+                ("isi_cv", C.c_double)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("rounds", C.c_int64), ("launches", C.c_int64), ("completed", C.c_int64), ("queued", C.c_int64),
+                ("resident", C.c_int64), ("events", C.c_int64), ("busy_ms", C.c_double), ("wall_ms", C.c_double),
+                ("bytes_in_use", C.c_int64), ("peak_bytes", C.c_int64)]
+
+
 # (name, restype, argtypes) of every exported entry point
 _P = C.c_void_p
 SIGNATURES = [
@@ -94,6 +111,8 @@ SIGNATURES = [
     ("g4s_net_set_geometry", C.c_int, [_P, C.c_int32]),
     ("g4s_net_get_geometry", C.c_int, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int64)]),
     ("g4s_nets_run", C.c_int, [_P, _P, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_int64)]),
+    ("g4s_net_autotune", C.c_int, [_P, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                   C.POINTER(C.c_double)]),
     ("g4s_net_destroy", C.c_int, [_P]),
     ("g4s_inject_fault", C.c_int, [_P, C.c_int32]),
     ("g4s_net_write_results", C.c_int, [_P, C.c_char_p, _P, C.c_double, C.c_double]),
@@ -101,6 +120,13 @@ SIGNATURES = [
                                    C.c_int32, C.c_char_p]),
     ("g4s_conn_glibc", C.c_int, [C.c_uint32, C.c_int32, C.c_int32, C.c_int32, _P, _P]),
     ("g4s_run_noalloc", C.c_int, [_P, C.c_int64, C.c_int32, C.c_int32, C.c_int32, _P, _P, _P, C.c_int64, _P, _P]),
+    ("g4s_server_start", C.c_int, [C.c_int64, C.c_int32, C.POINTER(_P)]),
+    ("g4s_server_submit", C.c_int, [_P, C.POINTER(Request), C.POINTER(C.c_int64)]),
+    ("g4s_server_poll", C.c_int, [_P, _P, C.c_int32, C.POINTER(C.c_int32)]),
+    ("g4s_server_result", C.c_int, [_P, C.c_int64, _P, _P, C.c_int64, C.POINTER(C.c_int64), _P, _P, _P]),
+    ("g4s_server_release", C.c_int, [_P, C.c_int64]),
+    ("g4s_server_get_stats", C.c_int, [_P, C.POINTER(ServerStats)]),
+    ("g4s_server_stop", C.c_int, [_P, C.c_int32]),
     ("g4s_pinned_alloc", C.c_int, [C.c_uint64, C.POINTER(_P)]),
     ("g4s_pinned_free", C.c_int, [_P]),
 ]

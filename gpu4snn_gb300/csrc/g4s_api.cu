@@ -16,7 +16,11 @@
 #include <cstdlib>
 #include <cstring>
 #include <fstream>
+#include <cmath>
+#include <map>
 #include <memory>
+#include <mutex>
+#include <tuple>
 #include <new>
 #include <string>
 #include <vector>
@@ -92,6 +96,12 @@ struct TeamLaunch {
   }
 };
 
+// A scheme and, for SKL, a team size chosen by the autotuner (0 = the default team).
+struct TuneChoice {
+  int alg = kAlgSKL;
+  int team = 0;
+};
+
 // ---------------------------------------------------------------------------------------
 // Handle.
 // ---------------------------------------------------------------------------------------
@@ -137,6 +147,9 @@ struct g4s_net {
   bool tables_fit = false;
   unsigned long long max_in = 0, max_mag = 0;
   TeamLaunch launch;
+  // autotuner: this handle's measured choice
+  bool tuned = false;
+  TuneChoice tune;
 };
 
 static std::atomic<int> g_fail_next_alloc{0};
@@ -363,13 +376,48 @@ int conn_glibc_host(unsigned seed, int32_t n, int32_t nsyn, int32_t stride, int3
 // ---------------------------------------------------------------------------------------
 // Step loop.
 // ---------------------------------------------------------------------------------------
+// ---------------------------------------------------------------------------------------
+// Autotuner.  Choices are cached process-wide by (log2 N, log2 Nsyn, log2 firing rate):
+// a scheme and, for SKL, the team size.  g4s_net_autotune measures the candidates on the
+// handle itself from a device snapshot of its state, restored afterwards, so tuning does
+// not change the simulation.  ALG_AUTO uses the handle's own choice, else the cached one
+// for its key (with the rate of its last run), else SKL with the default team.
+// ---------------------------------------------------------------------------------------
+static std::mutex g_tune_mu;
+static std::map<std::tuple<int, int, int>, TuneChoice> g_tune_cache;
+
+static int ilog2(double x) { return x < 1.0 ? 0 : (int)std::floor(std::log2(x)); }
+
+static std::tuple<int, int, int> tune_key(const g4s_net *n, double rate_hz) {
+  return std::make_tuple(ilog2((double)n->v.n), ilog2((double)n->v.nsyn), ilog2(rate_hz + 1.0));
+}
+
+static double recent_rate(const g4s_net *n) {
+  const size_t k = std::min<size_t>(n->counts.size(), 200);
+  if (!k) return 8.0;  // no history: assume the balanced regime
+  double s = 0;
+  for (size_t i = n->counts.size() - k; i < n->counts.size(); ++i) s += n->counts[i];
+  return s / (double)k / (double)n->v.n * 1000.0;
+}
+
 static int resolve_alg(g4s_net *n, int alg) {
-  if (alg == kAlgAuto) {
-    n->shape = DeliverShape{};
-    n->shape.group = 0;
-    return kAlgSKL;
+  if (alg != kAlgAuto) return alg;
+  n->shape = DeliverShape{};
+  n->shape.group = 0;
+  TuneChoice c;
+  if (n->tuned) {
+    c = n->tune;
+  } else {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune_cache.find(tune_key(n, recent_rate(n)));
+    if (it != g_tune_cache.end()) c = it->second;
   }
-  return alg;
+  if (c.alg == kAlgSKL && c.team != n->want_p && n->want_p == 0 && c.team > 0) {
+    n->want_p = c.team;
+    n->team_ready = false;
+    n->team_ok = true;
+  }
+  return c.alg;
 }
 
 // ---------------------------------------------------------------------------------------
@@ -707,6 +755,113 @@ static int run_nets(g4s_net *const *nets, const int32_t *steps, int count, doubl
 }
 
 // ---------------------------------------------------------------------------------------
+// Autotuner measurement: a device snapshot of the mutable state and the host record,
+// each candidate timed on `probe` steps from the snapshot, the snapshot restored.
+// Candidates: SKL with the default team and with teams of 1, 2, 4, ... CTAs up to the
+// co-resident grid (those that fit), AB and AP.
+// ---------------------------------------------------------------------------------------
+struct StateSnapshot {
+  float2 *vu = nullptr;
+  long long *acc = nullptr;
+  SpikeStat *ss = nullptr;
+  float *il = nullptr;
+  int64_t t_abs = 0, total = 0;
+  size_t nr = 0, nc = 0;
+  ~StateSnapshot() {
+    cudaFree(vu);
+    cudaFree(acc);
+    cudaFree(ss);
+    cudaFree(il);
+  }
+};
+
+static int snapshot_take(g4s_net *n, StateSnapshot &s) {
+  const size_t N = (size_t)n->v.n;
+  G4S_CUDA(cudaMalloc((void **)&s.vu, N * sizeof(float2)));
+  G4S_CUDA(cudaMalloc((void **)&s.acc, N * sizeof(long long)));
+  G4S_CUDA(cudaMalloc((void **)&s.ss, N * sizeof(SpikeStat)));
+  G4S_CUDA(cudaMalloc((void **)&s.il, N * sizeof(float)));
+  G4S_CUDA(cudaMemcpyAsync(s.vu, n->v.vu, N * sizeof(float2), cudaMemcpyDeviceToDevice, n->stream));
+  G4S_CUDA(cudaMemcpyAsync(s.acc, n->v.acc, N * sizeof(long long), cudaMemcpyDeviceToDevice, n->stream));
+  G4S_CUDA(cudaMemcpyAsync(s.ss, n->v.sstat, N * sizeof(SpikeStat), cudaMemcpyDeviceToDevice, n->stream));
+  G4S_CUDA(cudaMemcpyAsync(s.il, n->v.ilast, N * sizeof(float), cudaMemcpyDeviceToDevice, n->stream));
+  G4S_CUDA(cudaStreamSynchronize(n->stream));
+  s.t_abs = n->t_abs;
+  s.total = n->total_spikes;
+  s.nr = n->rt.size();
+  s.nc = n->counts.size();
+  return G4S_OK;
+}
+
+static int snapshot_restore(g4s_net *n, const StateSnapshot &s) {
+  const size_t N = (size_t)n->v.n;
+  G4S_CUDA(cudaMemcpyAsync(n->v.vu, s.vu, N * sizeof(float2), cudaMemcpyDeviceToDevice, n->stream));
+  G4S_CUDA(cudaMemcpyAsync(n->v.acc, s.acc, N * sizeof(long long), cudaMemcpyDeviceToDevice, n->stream));
+  G4S_CUDA(cudaMemcpyAsync(n->v.sstat, s.ss, N * sizeof(SpikeStat), cudaMemcpyDeviceToDevice, n->stream));
+  G4S_CUDA(cudaMemcpyAsync(n->v.ilast, s.il, N * sizeof(float), cudaMemcpyDeviceToDevice, n->stream));
+  G4S_CUDA(cudaStreamSynchronize(n->stream));
+  n->t_abs = s.t_abs;
+  n->total_spikes = s.total;
+  n->rt.resize(s.nr);
+  n->rid.resize(s.nr);
+  n->counts.resize(s.nc);
+  n->upd_ms.resize(s.nc);
+  n->step_ms.resize(s.nc);
+  return G4S_OK;
+}
+
+static int autotune(g4s_net *n, int32_t probe, TuneChoice *best, double *best_us) {
+  probe = std::max(8, std::min(probe, 4000));
+  StateSnapshot snap;
+  int rc = snapshot_take(n, snap);
+  if (rc) return rc;
+  const int keep_p = n->want_p;
+  std::vector<TuneChoice> cand;
+  cand.push_back(TuneChoice{kAlgSKL, 0});
+  int pmax = 0;
+  if (team_max_blocks(team_smem(1), &pmax) == cudaSuccess)
+    for (int p = 1; p <= pmax; p *= 2) cand.push_back(TuneChoice{kAlgSKL, p});
+  (void)cudaGetLastError();
+  if (pmax > 1) cand.push_back(TuneChoice{kAlgSKL, pmax});
+  cand.push_back(TuneChoice{kAlgAB, 0});
+  cand.push_back(TuneChoice{kAlgAP, 0});
+  double best_t = 1e300, rate = 0.0;
+  TuneChoice pick = cand[0];
+  for (const TuneChoice &c : cand) {
+    if (c.alg == kAlgSKL) {
+      n->want_p = c.team;
+      n->team_ready = false;
+      n->team_ok = true;
+      if ((rc = prepare_team(n))) break;
+      if (!n->team_ok || (c.team > 0 && n->team_p != c.team)) continue;  // does not fit
+    }
+    if ((rc = run_net(n, 8, c.alg)) || (rc = snapshot_restore(n, snap))) break;
+    if ((rc = run_net(n, probe, c.alg))) break;
+    const double t = n->last_kernel_ms * 1e3 / probe;
+    rate = (double)n->last_spikes / ((double)n->v.n * probe) * 1000.0;
+    if ((rc = snapshot_restore(n, snap))) break;
+    if (t < best_t) {
+      best_t = t;
+      pick = c;
+      if (c.alg == kAlgSKL && c.team == 0) pick.team = n->team_p;
+    }
+  }
+  n->want_p = keep_p;
+  n->team_ready = false;
+  n->team_ok = true;
+  if (rc) return rc;
+  n->tune = pick;
+  n->tuned = true;
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune_cache[tune_key(n, rate)] = pick;
+  }
+  *best = pick;
+  *best_us = best_t;
+  return G4S_OK;
+}
+
+// ---------------------------------------------------------------------------------------
 // Result files in the reference's formats.
 // ---------------------------------------------------------------------------------------
 static int mkdirs(const std::string &path) {
@@ -867,6 +1022,18 @@ int g4s_net_get_geometry(g4s_net *n, int32_t *owner_blocks, int64_t *slice) {
   const bool ok = n->team_ok && n->team_ready;
   if (owner_blocks) *owner_blocks = ok ? n->team_p : 0;
   if (slice) *slice = ok ? n->team_rc : 0;
+  return G4S_OK;
+}
+
+int g4s_net_autotune(g4s_net *n, int32_t probe_steps, int32_t *algorithm, int32_t *team, double *us_per_step) {
+  if (!n) return set_error(G4S_ERR_INVALID, "null handle");
+  TuneChoice c;
+  double us = 0.0;
+  int rc = autotune(n, probe_steps, &c, &us);
+  if (rc) return rc;
+  if (algorithm) *algorithm = c.alg;
+  if (team) *team = c.team;
+  if (us_per_step) *us_per_step = us;
   return G4S_OK;
 }
 

@@ -89,6 +89,13 @@ class Network:
         """SKL owner CTAs (0 = automatic)."""
         check(load().g4s_net_set_geometry(self._h, owner_blocks))
 
+    def autotune(self, probe_steps: int = 100) -> tuple[int, int, float]:
+        """Time the candidate schemes on this network (state restored afterwards) and keep
+        the fastest for ALG_AUTO.  Returns (scheme, team size, us per step)."""
+        a, t, us = C.c_int32(), C.c_int32(), C.c_double()
+        check(load().g4s_net_autotune(self._h, probe_steps, C.byref(a), C.byref(t), C.byref(us)))
+        return a.value, t.value, us.value
+
     def geometry(self) -> tuple[int, int]:
         """(owner CTAs, neurons per CTA) of the SKL kernel; (0, 0) on the fallback kernel."""
         p, rc = C.c_int32(), C.c_int64()

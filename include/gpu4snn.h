@@ -127,6 +127,14 @@ int g4s_net_set_barrier_timeout(g4s_net *net, uint64_t ns);
 int g4s_net_set_geometry(g4s_net *net, int32_t owner_blocks);
 int g4s_net_get_geometry(g4s_net *net, int32_t *owner_blocks, int64_t *slice);
 
+/* Autotuner (replaces the reference's occupancy-based launch configurator,
+ * gpu4snn.cu:780-838, 959-1079): times the candidate schemes (SKL with teams of 1, 2, 4, ...
+ * CTAs, AB, AP) on `probe_steps` steps of this network from a device snapshot of its state,
+ * restores the state (the simulation is unchanged), and keeps the fastest for ALG_AUTO on
+ * this handle and, process-wide, for networks of the same size, fan-out and firing rate
+ * (log2 buckets).  Outputs (any may be NULL): the scheme, its team size, us per step. */
+int g4s_net_autotune(g4s_net *net, int32_t probe_steps, int32_t *algorithm, int32_t *team, double *us_per_step);
+
 /* Batched execution (the reference runs one network per launch sequence; this has no
  * counterpart there beyond SKL_deliverspks, gpu4snn.cu:669-716): `count` independent
  * handles, network i advancing steps[i] further steps, all in shared persistent launches
@@ -157,6 +165,54 @@ int g4s_net_write_results(g4s_net *net, const char *dir, const float *init_state
  * network and write Results/N{n}Nsyn{nsyn}Regime{mode}Alg{alg}/ under results_root. */
 int g4s_run_protocol(int32_t n, int32_t nsyn, int32_t iterations, int32_t algorithm, int32_t mode, uint64_t seed,
                      int32_t conn_law, const char *results_root);
+
+/* Serving with continuous batching (no counterpart in the reference, which runs one
+ * experiment per process, gpu4snn.py:42).  A server admits submitted simulations while
+ * their estimated device bytes fit `hbm_budget_bytes`, keeps them resident, and advances
+ * all resident ones together by up to `quantum_steps` steps per persistent launch of the
+ * SKL team kernel; requests arriving meanwhile join at the next round.  submit/poll/
+ * result/release/get_stats are thread-safe. */
+typedef struct g4s_request {
+  int64_t n;           /* neurons                                   */
+  int32_t nsyn;        /* synapses per neuron                       */
+  int32_t steps;       /* steps to simulate                         */
+  uint64_t seed;       /* network seed                              */
+  float drive_scale;   /* thalamic gains (5, 2) x scale             */
+  int32_t record_raster;
+} g4s_request;
+
+typedef struct g4s_request_result {
+  int64_t id;
+  int32_t status;       /* 0 or G4S_ERR_*                            */
+  int32_t steps_done;
+  int64_t total_spikes;
+  double latency_ms;    /* submit -> results on the host             */
+  double queue_ms;      /* submit -> resident on the device          */
+  double rate_hz;       /* FP64 statistics of the run                */
+  double isi_cv;
+} g4s_request_result;
+
+typedef struct g4s_server_stats {
+  int64_t rounds, launches, completed, queued, resident, events;
+  double busy_ms;       /* CUDA-event time of the rounds' launches   */
+  double wall_ms;       /* since start                               */
+  int64_t bytes_in_use, peak_bytes;
+} g4s_server_stats;
+
+typedef struct g4s_server g4s_server;
+int g4s_server_start(int64_t hbm_budget_bytes, int32_t quantum_steps, g4s_server **out);
+/* G4S_ERR_BUDGET if the request alone exceeds the budget; G4S_ERR_INVALID if malformed. */
+int g4s_server_submit(g4s_server *s, const g4s_request *req, int64_t *id);
+/* Results completed since the last poll (up to cap). */
+int g4s_server_poll(g4s_server *s, g4s_request_result *out, int32_t cap, int32_t *n);
+/* Raster ((step, id) order) and final v, u, spike counts of a completed request. */
+int g4s_server_result(g4s_server *s, int64_t id, int32_t *t, int32_t *ids, int64_t cap, int64_t *n, float *v,
+                      float *u, int32_t *nospks);
+int g4s_server_release(g4s_server *s, int64_t id);
+int g4s_server_get_stats(g4s_server *s, g4s_server_stats *out);
+/* drain = 1: wait for every submitted request first; 0: finish the resident ones, drop
+ * the queued ones. */
+int g4s_server_stop(g4s_server *s, int32_t drain);
 
 /* Device arrays of one network, owned by the caller (layouts as the library's own). */
 typedef struct g4s_dev_net {
