@@ -196,6 +196,115 @@ def workload_config(name, cfg):
             "parallelism": "replicas"}
 
 
+ALG_LABEL = {0: "AP", 1: "N", 2: "S", 3: "AB", 4: "SKL", 5: "AUTO"}
+
+
+def schemes_leg(g, net, nsyn, steps):
+    """Each of the five schemes on the same network for `steps` steps (the simulation
+    continues from one scheme to the next; the dynamics are stationary)."""
+    out = {}
+    for alg in (0, 1, 2, 3, 4):
+        net.run(20, alg)
+        net.run(steps, alg)
+        inf = net.info()
+        out[ALG_LABEL[alg]] = {"events_per_s": inf.last_run_spikes * nsyn / (inf.last_run_ms * 1e-3),
+                               "us_per_step": inf.last_run_ms * 1e3 / steps, "steps": steps}
+    return out
+
+
+def ensemble(count, seed=5):
+    """The batched ensemble: N log-uniform in [1e3, 5e4], Nsyn uniform in [100, 2000]
+    (at most N-1), drive scale U(0.5, 2), steps uniform in [1000, 5000], own seeds."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    N = np.exp(rng.uniform(np.log(1000), np.log(50000), count)).astype(int)
+    S = np.minimum(rng.integers(100, 2001, count), N - 1)
+    D = rng.uniform(0.5, 2.0, count)
+    T = rng.integers(1000, 5001, count)
+    seeds = rng.integers(1, 2**62, count)
+    return N, S, D, T, seeds
+
+
+def batched_leg(g, count):
+    """All networks in shared persistent launches vs one network per launch, in turn."""
+    N, S, D, T, seeds = ensemble(count)
+    nets = [g.Network(int(n), int(s), seed=int(sd), drive_scale=float(d), record_raster=False)
+            for n, s, sd, d in zip(N, S, seeds, D)]
+    g.run_batch(nets, T.tolist())  # warm-up
+    for x in nets:
+        x.reset()
+    t0 = time.perf_counter()
+    ms, launches = g.run_batch(nets, T.tolist())
+    wall = time.perf_counter() - t0
+    ev = sum(x.info().last_run_spikes * int(s) for x, s in zip(nets, S))
+    counts_b = [x.info().last_run_spikes for x in nets]
+    for x in nets:
+        x.reset()
+    p_ms, p_ev = 0.0, 0
+    for x, t, s in zip(nets, T, S):
+        x.run(int(t), g.ALG_AUTO)
+        inf = x.info()
+        p_ms += inf.last_run_ms
+        p_ev += inf.last_run_spikes * int(s)
+    same = counts_b == [x.info().last_run_spikes for x in nets]
+    for x in nets:
+        x.close()
+    return {"networks": count, "synapses": int((N * S).sum()), "launches": int(launches),
+            "device_ms": ms, "wall_ms": wall * 1e3, "sims_per_s": count / (ms * 1e-3), "events_per_s": ev / (ms * 1e-3),
+            "plain_device_ms": p_ms, "plain_sims_per_s": count / (p_ms * 1e-3),
+            "plain_events_per_s": p_ev / (p_ms * 1e-3), "speedup_vs_plain": p_ms / ms,
+            "identical_spike_counts": same,
+            "workload": "N log-U[1e3,5e4], Nsyn U[100,2000] (<= N-1), drive U(0.5,2), steps U[1000,5000], seed 5"}
+
+
+def served_leg(g, count, lams):
+    """Poisson arrivals of simulation requests to the continuous-batching server (150 GB
+    budget), against serving the same requests one network per launch, in turn."""
+    import numpy as np
+    from gpu4snn_gb300.server import Server
+    rng = np.random.default_rng(6)
+    N = np.exp(rng.uniform(np.log(1e3), np.log(2e5), count)).astype(int)
+    S = np.minimum(rng.integers(100, 2001, count), N - 1)
+    T = np.exp(rng.uniform(np.log(500), np.log(2e4), count)).astype(int)
+    D = rng.uniform(0.5, 2.0, count)
+    seeds = rng.integers(1, 2**62, count)
+    out = {"requests": count, "workload": "N log-U[1e3,2e5], Nsyn U[100,2000] (<= N-1), steps log-U[500,2e4], "
+                                          "drive U(0.5,2), seed 6; budget 150 GB, quantum 250 steps"}
+    for lam in lams:
+        gaps = rng.exponential(1.0 / lam, count)
+        with Server(hbm_budget_bytes=150 << 30, quantum=250) as srv:
+            t0 = time.perf_counter()
+            for k in range(count):
+                while time.perf_counter() - t0 < gaps[:k + 1].sum():
+                    time.sleep(0.0002)
+                srv.submit(int(N[k]), int(S[k]), int(T[k]), int(seeds[k]), float(D[k]))
+            res = {}
+            while len(res) < count:
+                for r in srv.poll():
+                    res[r.id] = r
+                time.sleep(0.001)
+            wall = time.perf_counter() - t0
+            st = srv.stats()
+        lat = np.array([r.latency_ms for r in res.values()])
+        out[f"lambda_{lam:g}"] = {"req_per_s": count / wall, "events_per_s": st.events / wall,
+                                  "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                                  "rounds": int(st.rounds), "gpu_busy_ms": st.busy_ms,
+                                  "peak_gib": st.peak_bytes / 2**30, "failed": int(sum(r.status != 0 for r in res.values()))}
+    t0 = time.perf_counter()
+    lat = []
+    for k in range(count):
+        ts = time.perf_counter()
+        with g.Network(int(N[k]), int(S[k]), seed=int(seeds[k]), drive_scale=float(D[k]), record_raster=False) as x:
+            x.run(int(T[k]), g.ALG_AUTO)
+        lat.append((time.perf_counter() - ts) * 1e3)
+    wall = time.perf_counter() - t0
+    out["plain"] = {"req_per_s": count / wall, "p50_service_ms": float(np.percentile(lat, 50)),
+                    "p99_service_ms": float(np.percentile(lat, 99))}
+    best = max(v["req_per_s"] for k, v in out.items() if k.startswith("lambda_"))
+    out["speedup_vs_plain"] = best / out["plain"]["req_per_s"]
+    return out
+
+
 def load_traffic(name):
     p = os.path.join(ROOT, "profiles", "persistent_step_traffic.json")
     if os.path.exists(p):
@@ -215,6 +324,11 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
     ap.add_argument("--raster-budget-mb", type=int, default=0, help="device raster buffer per chunk (0: default)")
+    ap.add_argument("--no-schemes", action="store_true", help="skip timing the five schemes one by one")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched-ensemble leg")
+    ap.add_argument("--batch-networks", type=int, default=256, help="networks of the batched ensemble")
+    ap.add_argument("--served", default="", help="comma-separated Poisson arrival rates (req/s) for the served leg")
+    ap.add_argument("--served-requests", type=int, default=200, help="requests per arrival rate")
     a = ap.parse_args()
     if a.warmup < 3:
         a.warmup = 3
@@ -231,6 +345,13 @@ def main():
     alg = g.ALG_NAMES[a.algorithm.upper()] if not a.algorithm.isdigit() else int(a.algorithm)
     budget = a.raster_budget_mb << 20
     net = g.Network(n, nsyn, seed=seed, drive_scale=drive, record_raster=False, raster_budget_bytes=budget)
+    schemes = None
+    if not a.no_schemes:
+        schemes = schemes_leg(g, net, nsyn, min(T, 500))
+    tuned = None
+    if alg == g.ALG_AUTO:
+        talg, tteam, tus = net.autotune(min(T, 200))
+        tuned = {"algorithm": talg, "name": ALG_LABEL[talg], "team": tteam, "us_per_step": tus}
     for _ in range(a.warmup):
         net.run(T, alg)
     runs = []
@@ -263,7 +384,15 @@ def main():
     achieved = (deliv_bytes + upd_bytes) / n_launch / (kern_ms / n_launch * 1e-3) / 1e9
     upd_ms = sum(r[4] for r in runs)
     deliv_ms = max(1e-9, sum(r[5] for r in runs) - upd_ms)
-    roofline = {"kernel": "k_persistent (SKL: fused update + delivery, all steps of a chunk)", "bound": "hbm",
+    team, slice_ = net.geometry()
+    last_alg = int(runs[-1][6])
+    if last_alg == g.ALG_SKL and team > 0:
+        kname = f"k_team (SKL team kernel: {team} CTAs x 1024 threads, {slice_} neurons per CTA)"
+    elif last_alg == g.ALG_SKL:
+        kname = "k_persistent (SKL global-atomic kernel)"
+    else:
+        kname = f"k_update + k_deliver ({ALG_LABEL[last_alg]})"
+    roofline = {"kernel": kname, "bound": "hbm",
                 "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "peak_source": f"{peak_kind} hbm_gbs", "traffic": load_traffic(a.workload),
                 "algorithmic_bytes_per_launch": (deliv_bytes + upd_bytes) / n_launch,
@@ -274,7 +403,8 @@ def main():
     line = {"metric": "synaptic events/s", "value": value, "unit": "events/s", "n_gpus": ws, "steps": a.steps,
             "warmup": a.warmup, "ms_per_step": t_max / a.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32+i64", "data": "synthetic (seeded Philox network)",
-            "config": workload_config(a.workload, cfg), "algorithm": int(runs[-1][6]),
+            "config": workload_config(a.workload, cfg), "algorithm": ALG_LABEL[last_alg],
+            "autotuned": tuned, "schemes": schemes,
             "firing_rate_hz": spikes / (n * T * a.steps) * 1000.0, "wall_s": wall,
             "roofline": roofline, "clocks": clocks, "gpu_launches": int(launches)}
     # end to end through the C ABI with host buffers
@@ -316,6 +446,10 @@ def main():
         line["cpu_baseline"] = {"value": v, "unit": "events/s", "cores": threads, "kind": "port",
                                 "sample": f"{st} simulation steps after 100 warm-up steps of the same network "
                                           f"({dt:.1f} s), oracle OpenMP port"}
+    if rank == 0 and ws == 1 and not a.no_batched:
+        line["batched"] = batched_leg(g, a.batch_networks)
+    if rank == 0 and ws == 1 and a.served:
+        line["served"] = served_leg(g, a.served_requests, [float(x) for x in a.served.split(",")])
     if rank == 0:
         print(json.dumps(line), flush=True)
     return 0

@@ -100,6 +100,7 @@ struct TeamLaunch {
 struct TuneChoice {
   int alg = kAlgSKL;
   int team = 0;
+  int mode = kDeliverRun;
 };
 
 // ---------------------------------------------------------------------------------------
@@ -139,11 +140,13 @@ struct g4s_net {
   int team_p = 0;
   int64_t team_rc = 0;
   bool team_ready = false;
+  bool team_batch = false;  // geometry planned for a multi-network batch
   bool team_ok = true;
   int *list = nullptr;
   uint16_t *seg = nullptr;
   size_t seg_bytes = 0;
   int want_p = 0;
+  int deliver_mode = kDeliverRun;
   bool tables_fit = false;
   unsigned long long max_in = 0, max_mag = 0;
   TeamLaunch launch;
@@ -417,6 +420,7 @@ static int resolve_alg(g4s_net *n, int alg) {
     n->team_ready = false;
     n->team_ok = true;
   }
+  if (c.alg == kAlgSKL) n->deliver_mode = c.mode;
   return c.alg;
 }
 
@@ -427,7 +431,7 @@ static int resolve_alg(g4s_net *n, int alg) {
 // Returns false if the network does not fit or its tables break the exactness bound of
 // the split accumulation (the global-atomic persistent kernel is used instead).
 // ---------------------------------------------------------------------------------------
-static bool plan_team(g4s_net *n, int want, int *p_out, int64_t *rc_out) {
+static bool plan_team(g4s_net *n, int want, bool batch, int *p_out, int64_t *rc_out) {
   const NetView &v = n->v;
   if (!n->tables_fit) return false;
   const int64_t rc_cap = (int64_t)((kTeamSmemLimit - 16) / 12);
@@ -436,7 +440,9 @@ static bool plan_team(g4s_net *n, int want, int *p_out, int64_t *rc_out) {
     (void)cudaGetLastError();
     return false;
   }
-  int64_t p = want > 0 ? want : (v.n + 2047) / 2048;
+  // alone, a network spreads over the GPU (one CTA per 2048 neurons); in a batch it takes
+  // the fewest CTAs its slices fit in, so that more networks run at once
+  int64_t p = want > 0 ? want : (batch ? (v.n + kBatchSlice - 1) / kBatchSlice : (v.n + kSoloSlice - 1) / kSoloSlice);
   if (p < 1) p = 1;
   if (p > pmax) p = pmax;
   int64_t rc = (v.n + p - 1) / p;
@@ -457,11 +463,12 @@ static bool plan_team(g4s_net *n, int want, int *p_out, int64_t *rc_out) {
 
 // Team geometry, the per-step spike lists and, for teams of more than one CTA, the
 // per-row segment table.
-static int prepare_team(g4s_net *n) {
-  if (n->team_ready) return G4S_OK;
+static int prepare_team(g4s_net *n, bool batch = false) {
+  if (n->team_ready && n->team_batch == batch) return G4S_OK;
   int p = 0;
   int64_t rc = 0;
-  if (!plan_team(n, n->want_p, &p, &rc)) {
+  n->team_batch = batch;
+  if (!plan_team(n, n->want_p, batch, &p, &rc)) {
     n->team_ok = false;
     return G4S_OK;
   }
@@ -520,19 +527,32 @@ static int finish_tables(g4s_net *n) {
 
 // Results of one chunk of `cs` steps: per-step counts, raster offsets and stamps, and the
 // raster itself when recorded; each step's ids sorted (the device order is by CTA).
-static int absorb_chunk(g4s_net *n, int cs, int64_t *spikes) {
+// The three steps of absorbing a chunk, so that a batch can enqueue every network's
+// copies on one stream and synchronise once: per-step metadata, then the raster of the
+// networks that record it, then the host-side bookkeeping.
+static int chunk_copy_meta(g4s_net *n, int cs, cudaStream_t s) {
   NetView &v = n->v;
-  G4S_CUDA(cudaMemcpyAsync(n->h_counts, v.counts, (size_t)cs * 4, cudaMemcpyDeviceToHost, n->stream));
-  G4S_CUDA(cudaMemcpyAsync(n->h_base, v.base, (size_t)cs * 8, cudaMemcpyDeviceToHost, n->stream));
-  G4S_CUDA(cudaMemcpyAsync(n->h_stamps, v.stamps, (size_t)cs * 16, cudaMemcpyDeviceToHost, n->stream));
-  G4S_CUDA(cudaStreamSynchronize(n->stream));
-  const int64_t chunk_total = (int64_t)n->h_base[cs - 1] + n->h_counts[cs - 1];
-  if (n->desc.record_raster && chunk_total > 0) {
-    G4S_CUDA(cudaMemcpyAsync(n->h_raster, v.raster, (size_t)chunk_total * 4, cudaMemcpyDeviceToHost, n->stream));
-    G4S_CUDA(cudaStreamSynchronize(n->stream));
+  G4S_CUDA(cudaMemcpyAsync(n->h_counts, v.counts, (size_t)cs * 4, cudaMemcpyDeviceToHost, s));
+  G4S_CUDA(cudaMemcpyAsync(n->h_base, v.base, (size_t)cs * 8, cudaMemcpyDeviceToHost, s));
+  G4S_CUDA(cudaMemcpyAsync(n->h_stamps, v.stamps, (size_t)cs * 16, cudaMemcpyDeviceToHost, s));
+  return G4S_OK;
+}
+
+static int64_t chunk_total(const g4s_net *n, int cs) { return (int64_t)n->h_base[cs - 1] + n->h_counts[cs - 1]; }
+
+static int chunk_copy_raster(g4s_net *n, int cs, cudaStream_t s) {
+  const int64_t total = chunk_total(n, cs);
+  if (n->desc.record_raster && total > 0)
+    G4S_CUDA(cudaMemcpyAsync(n->h_raster, n->v.raster, (size_t)total * 4, cudaMemcpyDeviceToHost, s));
+  return G4S_OK;
+}
+
+static void chunk_finish(g4s_net *n, int cs, int64_t *spikes) {
+  const int64_t total = chunk_total(n, cs);
+  if (n->desc.record_raster && total > 0) {
     const size_t off = n->rt.size();
-    n->rt.resize(off + (size_t)chunk_total);
-    n->rid.resize(off + (size_t)chunk_total);
+    n->rt.resize(off + (size_t)total);
+    n->rid.resize(off + (size_t)total);
     for (int lt = 0; lt < cs; ++lt) {
       int *b = n->h_raster + n->h_base[lt];
       std::sort(b, b + n->h_counts[lt]);
@@ -550,8 +570,20 @@ static int absorb_chunk(g4s_net *n, int cs, int64_t *spikes) {
     n->upd_ms.push_back(s1 > s0 ? (float)((s1 - s0) * 1e-6) : 0.0f);
     n->step_ms.push_back(s2 > s0 ? (float)((s2 - s0) * 1e-6) : 0.0f);
   }
-  *spikes = chunk_total;
+  *spikes = total;
   n->t_abs += cs;
+}
+
+// Results of one chunk of `cs` steps of one network: per-step counts, raster offsets and
+// stamps, and the raster itself when recorded; each step's ids sorted (the device order
+// is by CTA).
+static int absorb_chunk(g4s_net *n, int cs, int64_t *spikes) {
+  int rc = chunk_copy_meta(n, cs, n->stream);
+  if (rc) return rc;
+  G4S_CUDA(cudaStreamSynchronize(n->stream));
+  if ((rc = chunk_copy_raster(n, cs, n->stream))) return rc;
+  G4S_CUDA(cudaStreamSynchronize(n->stream));
+  chunk_finish(n, cs, spikes);
   return G4S_OK;
 }
 
@@ -594,6 +626,7 @@ static int team_round(g4s_net *const *nets, const int *steps, const bool *last, 
     it.team = n->team_p;
     it.rc = (int)n->team_rc;
     it.sync = n->gs;
+    it.mode = n->deliver_mode;
     for (int r = 0; r < n->team_p; ++r) L.h_slots[k++] = make_int2(i, r);
     G4S_CUDA(cudaMemsetAsync(n->v.counts, 0, (size_t)steps[i] * sizeof(int), s));
     G4S_CUDA(cudaMemsetAsync(n->v.stamps, 0, ((size_t)steps[i] * 2 + 2) * 8, s));
@@ -707,7 +740,7 @@ static int run_nets(g4s_net *const *nets, const int32_t *steps, int count, doubl
       return set_error(G4S_ERR_INVALID, "bad step count in batch");
     for (int j = 0; j < i; ++j)
       if (nets[j] == nets[i]) return set_error(G4S_ERR_INVALID, "a handle appears twice in the batch");
-    int rc = prepare_team(nets[i]);
+    int rc = prepare_team(nets[i], count > 1);
     if (rc) return rc;
     if (!nets[i]->team_ok)
       return set_error(G4S_ERR_INVALID, "a network of the batch does not fit the team kernel");
@@ -732,10 +765,15 @@ static int run_nets(g4s_net *const *nets, const int32_t *steps, int count, doubl
     int rc = team_round(nets, cs.data(), last.get(), count, L, s, nets[0]->barrier_ns, 0, &kms, &nl);
     if (rc) return rc;
     for (int i = 0; i < count; ++i)
+      if (cs[i] > 0 && (rc = chunk_copy_meta(nets[i], cs[i], s))) return rc;
+    G4S_CUDA(cudaStreamSynchronize(s));
+    for (int i = 0; i < count; ++i)
+      if (cs[i] > 0 && (rc = chunk_copy_raster(nets[i], cs[i], s))) return rc;
+    G4S_CUDA(cudaStreamSynchronize(s));
+    for (int i = 0; i < count; ++i)
       if (cs[i] > 0) {
         int64_t sp = 0;
-        rc = absorb_chunk(nets[i], cs[i], &sp);
-        if (rc) return rc;
+        chunk_finish(nets[i], cs[i], &sp);
         nets[i]->last_spikes += sp;
         nets[i]->total_spikes += sp;
         remaining[i] -= cs[i];
@@ -817,19 +855,25 @@ static int autotune(g4s_net *n, int32_t probe, TuneChoice *best, double *best_us
   if (rc) return rc;
   const int keep_p = n->want_p;
   std::vector<TuneChoice> cand;
-  cand.push_back(TuneChoice{kAlgSKL, 0});
   int pmax = 0;
-  if (team_max_blocks(team_smem(1), &pmax) == cudaSuccess)
-    for (int p = 1; p <= pmax; p *= 2) cand.push_back(TuneChoice{kAlgSKL, p});
+  if (team_max_blocks(team_smem(1), &pmax) != cudaSuccess) pmax = 1;
   (void)cudaGetLastError();
-  if (pmax > 1) cand.push_back(TuneChoice{kAlgSKL, pmax});
-  cand.push_back(TuneChoice{kAlgAB, 0});
-  cand.push_back(TuneChoice{kAlgAP, 0});
+  std::vector<int> teams = {0};
+  for (int p = 1; p <= pmax; p *= 2) teams.push_back(p);
+  if (pmax > 1) teams.push_back(pmax);
+  for (int p : teams) {
+    cand.push_back(TuneChoice{kAlgSKL, p, kDeliverRun});
+    if (p != 1) cand.push_back(TuneChoice{kAlgSKL, p, kDeliverLane});
+  }
+  cand.push_back(TuneChoice{kAlgAB, 0, kDeliverRun});
+  cand.push_back(TuneChoice{kAlgAP, 0, kDeliverRun});
+  const int keep_mode = n->deliver_mode;
   double best_t = 1e300, rate = 0.0;
   TuneChoice pick = cand[0];
   for (const TuneChoice &c : cand) {
     if (c.alg == kAlgSKL) {
       n->want_p = c.team;
+      n->deliver_mode = c.mode;
       n->team_ready = false;
       n->team_ok = true;
       if ((rc = prepare_team(n))) break;
@@ -847,6 +891,7 @@ static int autotune(g4s_net *n, int32_t probe, TuneChoice *best, double *best_us
     }
   }
   n->want_p = keep_p;
+  n->deliver_mode = keep_mode;
   n->team_ready = false;
   n->team_ok = true;
   if (rc) return rc;
@@ -1006,10 +1051,13 @@ int g4s_net_load_tables(g4s_net *n, const int32_t *idx, const float *w, int32_t 
   return finish_tables(n);
 }
 
-int g4s_net_set_geometry(g4s_net *n, int32_t owner_blocks) {
+int g4s_net_set_geometry(g4s_net *n, int32_t owner_blocks, int32_t delivery) {
   if (!n) return set_error(G4S_ERR_INVALID, "null handle");
   if (owner_blocks < 0) return set_error(G4S_ERR_INVALID, "owner_blocks must be >= 0 (0 = automatic)");
+  if (delivery != kDeliverRun && delivery != kDeliverLane)
+    return set_error(G4S_ERR_INVALID, "delivery must be 0 (segment runs) or 1 (lane per spike)");
   n->want_p = owner_blocks;
+  n->deliver_mode = delivery;
   n->team_ready = false;
   n->team_ok = true;
   return G4S_OK;

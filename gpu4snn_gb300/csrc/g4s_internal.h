@@ -36,6 +36,10 @@ int persistent_blocks();
 // SKL team kernel (g4s_team.cu).
 constexpr int kMaxSortedNsyn = 16384;          // rows are sorted in shared memory
 constexpr size_t kTeamSmemLimit = 200 * 1024;  // shared memory per CTA for currents + spikes
+constexpr int64_t kPrezSlice = 12288;          // slices up to this size precompute the next drive
+constexpr int64_t kSoloSlice = 2048;           // neurons per CTA of a network running alone
+constexpr int64_t kBatchSlice = 2048;          // neurons per CTA of a batched network (measured: fewer,
+                                               // larger slices made the config-4 ensemble 1.4x slower)
 cudaError_t launch_sort_rows(const NetView &v, cudaStream_t s);
 cudaError_t launch_segoff(const NetView &v, int team, int64_t rc, uint16_t *seg, cudaStream_t s);
 cudaError_t launch_inbound(const NetView &v, unsigned *cnt, unsigned long long *mag, unsigned long long *out,

@@ -20,7 +20,8 @@
 //
 // Per step, for each team:
 //   update    every rank updates its own neurons (current read from and cleared in shared
-//             memory) and collects its spikes in shared memory;
+//             memory; drive precomputed in shared memory during the previous step) and
+//             collects its spikes in shared memory;
 //   exchange  one-CTA team: nothing, the spike list stays in shared memory.  Larger team:
 //             each rank appends its spikes to the network's global list of the step (two
 //             lists, by step parity), then a team barrier with a bounded spin;
@@ -30,6 +31,8 @@
 //             a per-row offset table gives the segment): a warp takes 32 spikes, scans
 //             their segment lengths and walks the concatenated segments, eight synapses
 //             per lane in flight.  Each weight goes into the rank's own shared memory.
+//   tail      once its delivery share is done, each thread updates the spike statistics
+//             of this CTA's spikes and computes the next step's drive of its neurons.
 //   The raster records the spike ids of every step while its buffer has room.
 #include <cuda_runtime.h>
 
@@ -151,6 +154,9 @@ __device__ void team_run(const TeamItem &it, int rank, unsigned char *s_raw, int
   int *s_a = reinterpret_cast<int *>(s_raw);
   unsigned *s_b = reinterpret_cast<unsigned *>(s_raw + (size_t)rc * 4);
   int *s_spk = reinterpret_cast<int *>(s_raw + (size_t)rc * 8);
+  // drive of the next step, computed during this step's delivery (slices up to kPrezSlice)
+  float *s_z = reinterpret_cast<float *>(s_raw + (size_t)rc * 12);
+  const bool prez = rc <= kPrezSlice;
   const int64_t lo = min((int64_t)rank * rc, v.n);
   const int64_t hi = min(lo + rc, v.n);
   const int cnt = (int)(hi - lo);
@@ -195,8 +201,9 @@ __device__ void team_run(const TeamItem &it, int rank, unsigned char *s_raw, int
         s_a[i1] = 0;
         s_b[i1] = 0;
       }
-      const float z0 = normal(v.seed, (uint64_t)n0, (uint64_t)t_abs);
-      const float z1 = normal(v.seed, (uint64_t)n1, (uint64_t)t_abs);
+      const bool use_z = prez && lt > 0;
+      const float z0 = use_z ? s_z[i0] : normal(v.seed, (uint64_t)n0, (uint64_t)t_abs);
+      const float z1 = use_z ? (h1 ? s_z[i1] : 0.0f) : normal(v.seed, (uint64_t)n1, (uint64_t)t_abs);
       float I0, I1;
       const bool k0 = izh_step(s0.x, s0.y, I0, p0, n0 < v.nexc ? v.ge : v.gi, z0, a0);
       const bool k1 = izh_step(s1.x, s1.y, I1, p1, n1 < v.nexc ? v.ge : v.gi, z1, a1) && h1;
@@ -206,23 +213,8 @@ __device__ void team_run(const TeamItem &it, int rank, unsigned char *s_raw, int
         v.ilast[n0] = I0;
         if (h1) v.ilast[n1] = I1;
       }
-#pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        const bool spk = h ? k1 : k0;
-        if (!spk) continue;
-        const int64_t n = h ? n1 : n0;
-        SpikeStat st = v.sstat[n];
-        st.nospks += 1;
-        if (st.last >= 0) {
-          const long long isi = t_abs - st.last;
-          st.nisi += 1;
-          st.s1 += isi;
-          st.s2 += isi * isi;
-        }
-        st.last = (int)t_abs;
-        v.sstat[n] = st;
-        s_spk[atomicAdd(s_nspk, 1)] = (int)n;
-      }
+      if (k0) s_spk[atomicAdd(s_nspk, 1)] = (int)n0;
+      if (k1) s_spk[atomicAdd(s_nspk, 1)] = (int)n1;
     }
     __syncthreads();
     const int nspk = *s_nspk;
@@ -272,6 +264,50 @@ __device__ void team_run(const TeamItem &it, int rank, unsigned char *s_raw, int
         if (j >= rv) {
           j -= rv;
           q += 1;
+        }
+      }
+    } else if (it.mode == kDeliverLane) {
+      // ---- delivery, larger team, one lane per spike: each lane walks its own segment,
+      // four synapses (eight loads) at a time; the warp's next 32 spike ids and segment
+      // bounds are loaded while the current ones are walked.  No shuffles: the shared-
+      // memory pipe carries only the atomics.
+      int q = warp * 32 + lane;
+      int s = 0, b = 0, e = 0;
+      if (q < K) {
+        s = __ldcg(glist + q);
+        const uint16_t *so = it.seg + (size_t)s * segw + rank;
+        b = so[0];
+        e = so[1];
+      }
+      for (int q0 = warp * 32; q0 < K; q0 += kWarps * 32) {
+        const int *ri = v.idx + (size_t)s * v.stride;
+        const float *rw = v.w + (size_t)s * v.stride;
+        const int cb = b, ce = e;
+        q = q0 + kWarps * 32 + lane;
+        s = 0;
+        b = 0;
+        e = 0;
+        if (q < K) {
+          s = __ldcg(glist + q);
+          const uint16_t *so = it.seg + (size_t)s * segw + rank;
+          b = so[0];
+          e = so[1];
+        }
+        for (int j = cb; j < ce; j += 4) {
+          int t[4];
+          float w[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            t[u] = -1;
+            w[u] = 0.0f;
+            if (j + u < ce) {
+              t[u] = __ldg(ri + j + u);
+              w[u] = __ldg(rw + j + u);
+            }
+          }
+#pragma unroll
+          for (int u = 0; u < 4; ++u)
+            if (t[u] >= 0) acc_add(base_a, base_b, (unsigned)(t[u] - (int)lo), wfix(w[u]));
         }
       }
     } else {
@@ -334,6 +370,23 @@ __device__ void team_run(const TeamItem &it, int rank, unsigned char *s_raw, int
         }
       }
     }
+    // ---- off the critical path, by each thread once its delivery share is done: the
+    // spike statistics of this CTA's spikes, and the next step's drive
+    for (int j = threadIdx.x; j < nspk; j += NT) {
+      const int n = s_spk[j];
+      SpikeStat st = v.sstat[n];
+      st.nospks += 1;
+      if (st.last >= 0) {
+        const long long isi = t_abs - st.last;
+        st.nisi += 1;
+        st.s1 += isi;
+        st.s2 += isi * isi;
+      }
+      st.last = (int)t_abs;
+      v.sstat[n] = st;
+    }
+    if (prez && lt + 1 < it.steps)
+      for (int i = threadIdx.x; i < cnt; i += NT) s_z[i] = normal(v.seed, (uint64_t)(lo + i), (uint64_t)(t_abs + 1));
     __syncthreads();
     base += K;
   }
@@ -369,7 +422,7 @@ __global__ void __launch_bounds__(NT, 1) k_team(const TeamItem *__restrict__ ite
 // ---------------------------------------------------------------------------------------
 constexpr int kTeamNT = 1024;
 
-size_t team_smem(int64_t rc) { return (size_t)rc * 12 + 16; }
+size_t team_smem(int64_t rc) { return (size_t)rc * (rc <= kPrezSlice ? 16 : 12) + 16; }
 
 cudaError_t team_max_blocks(size_t smem, int *out) {
   cudaError_t e = cudaFuncSetAttribute(k_team<kTeamNT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

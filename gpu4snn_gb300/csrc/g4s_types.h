@@ -68,6 +68,13 @@ struct TeamItem {
   int team;             // CTAs of the team
   int rc;               // neurons per CTA slice
   GridSync *sync;       // team barrier and error word
+  int mode;             // delivery mapping of a multi-CTA team (kDeliverRun or kDeliverLane)
+  int pad;
 };
+
+// Delivery mappings of a multi-CTA team: warps walk the concatenated segments of 32
+// spikes (kDeliverRun), or each lane walks one spike's segment (kDeliverLane).
+constexpr int kDeliverRun = 0;
+constexpr int kDeliverLane = 1;
 
 }  // namespace g4s

@@ -85,9 +85,9 @@ class Network:
     def inject_fault(self, kind: int):
         check(load().g4s_inject_fault(self._h, kind))
 
-    def set_geometry(self, owner_blocks: int = 0):
-        """SKL owner CTAs (0 = automatic)."""
-        check(load().g4s_net_set_geometry(self._h, owner_blocks))
+    def set_geometry(self, owner_blocks: int = 0, delivery: int = 0):
+        """SKL owner CTAs (0 = automatic) and delivery mapping (0 segment runs, 1 lane per spike)."""
+        check(load().g4s_net_set_geometry(self._h, owner_blocks, delivery))
 
     def autotune(self, probe_steps: int = 100) -> tuple[int, int, float]:
         """Time the candidate schemes on this network (state restored afterwards) and keep

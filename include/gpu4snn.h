@@ -120,11 +120,13 @@ int g4s_net_stats(g4s_net *net, double *rate_hz, double *isi_cv, int64_t *total_
 int g4s_net_set_barrier_timeout(g4s_net *net, uint64_t ns);
 /* Geometry of the SKL kernel (the reference sizes its persistent grids from occupancy,
  * gpu4snn.cu:1066-1076): `owner_blocks` CTAs, each owning a contiguous slice of target
- * neurons whose currents stay in its shared memory; 0 = automatic.  get_geometry reports
- * the geometry in use (zeros when the network is too large for shared-memory ownership,
- * or its tables exceed the exact-accumulation bound, and the global-atomic persistent
- * kernel runs instead) and the neurons per CTA. */
-int g4s_net_set_geometry(g4s_net *net, int32_t owner_blocks);
+ * neurons whose currents stay in its shared memory (0 = automatic), and the delivery
+ * mapping of a multi-CTA team (0: warps walk the concatenated segments of 32 spikes;
+ * 1: one lane per spike).  get_geometry reports the geometry in use (zeros when the
+ * network is too large for shared-memory ownership, or its tables exceed the
+ * exact-accumulation bound, and the global-atomic persistent kernel runs instead) and the
+ * neurons per CTA. */
+int g4s_net_set_geometry(g4s_net *net, int32_t owner_blocks, int32_t delivery);
 int g4s_net_get_geometry(g4s_net *net, int32_t *owner_blocks, int64_t *slice);
 
 /* Autotuner (replaces the reference's occupancy-based launch configurator,

@@ -149,16 +149,18 @@ def test_barrier_timeout_is_reported(g4s, oracle):
         assert np.array_equal(np.stack(net.raster()), np.stack(sim.raster()))
 
 
-@pytest.mark.parametrize("p,n", [(1, 2500), (2, 2500), (3, 3001), (7, 5003), (152, 4099), (0, 20011), (40, 9000)])
-def test_owner_geometries(g4s, oracle, p, n):
+@pytest.mark.parametrize("p,n,mode", [(1, 2500, 0), (2, 2500, 0), (3, 3001, 1), (7, 5003, 0), (152, 4099, 1),
+                                      (0, 20011, 0), (0, 20011, 1), (40, 9000, 1)])
+def test_owner_geometries(g4s, oracle, p, n, mode):
     """The owner-computes SKL kernel under forced geometries (one CTA, odd counts, more
-    CTAs than 2048-neuron slices, slices that do not divide N) against the oracle."""
+    CTAs than 2048-neuron slices, slices that do not divide N) and both delivery mappings
+    of a multi-CTA team, against the oracle."""
     nsyn, seed = 300, 21
     d, (idx, w) = oracle_tables(oracle, n, nsyn, seed)
     sim = oracle.Sim(d, idx, w)
     sim.run(120, threads=8)
     with g4s.Network(n, nsyn, seed=seed) as net:
-        net.set_geometry(p)
+        net.set_geometry(p, mode)
         gp, rc = net.geometry()
         assert (p == 0 or gp == p) and rc > 0
         net.run(70, 4)
