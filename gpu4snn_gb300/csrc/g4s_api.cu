@@ -118,6 +118,7 @@ struct g4s_net {
   int64_t chunk_steps = 0;   // steps per chunk of the team kernel
   int64_t chunk_legacy = 0;  // steps per chunk of the other kernels (raster = spike list)
   int64_t t_abs = 0;
+  uint32_t tag_next = 0;  // record tags of the team kernel: never repeated for this handle's lists
   unsigned long long barrier_ns = 2000000000ull;
   size_t device_bytes = 0;
   // pinned staging of one chunk
@@ -142,7 +143,7 @@ struct g4s_net {
   bool team_ready = false;
   bool team_batch = false;  // geometry planned for a multi-network batch
   bool team_ok = true;
-  int *list = nullptr;
+  unsigned long long *list = nullptr;
   uint16_t *seg = nullptr;
   size_t seg_bytes = 0;
   int want_p = 0;
@@ -272,7 +273,8 @@ static int alloc_net(const g4s_net_desc *d, g4s_net **out) {
       (rc = dalloc(n, &v.raster, (size_t)v.raster_cap, "raster")) ||
       (rc = dalloc(n, &v.counts, (size_t)cs, "counts")) || (rc = dalloc(n, &v.base, (size_t)cs, "offsets")) ||
       (rc = dalloc(n, &v.stamps, (size_t)cs * 2 + 2, "stamps")) || (rc = dalloc(n, &v.status, 1, "status")) ||
-      (rc = dalloc(n, &n->gs, 1, "barrier")) || (rc = dalloc(n, &n->d_stats, 2, "stats"))) {
+      (rc = dalloc(n, &n->gs, 1 + 2 * (size_t)kMaxTeam * kRecLines, "barrier and spike records")) ||
+      (rc = dalloc(n, &n->d_stats, 2, "stats"))) {
     free_net(n);
     return rc;
   }
@@ -434,25 +436,25 @@ static int resolve_alg(g4s_net *n, int alg) {
 static bool plan_team(g4s_net *n, int want, bool batch, int *p_out, int64_t *rc_out) {
   const NetView &v = n->v;
   if (!n->tables_fit) return false;
-  const int64_t rc_cap = (int64_t)((kTeamSmemLimit - 16) / 12);
   int pmax = 0;
-  if (team_max_blocks(team_smem(std::min<int64_t>(rc_cap, v.n)), &pmax) != cudaSuccess || pmax < 1) {
+  if (team_max_blocks(kTeamSmemLimit, &pmax) != cudaSuccess || pmax < 1) {
     (void)cudaGetLastError();
     return false;
   }
+  pmax = std::min(pmax, kMaxTeam);
   // alone, a network spreads over the GPU (one CTA per 2048 neurons); in a batch it takes
   // the fewest CTAs its slices fit in, so that more networks run at once
   int64_t p = want > 0 ? want : (batch ? (v.n + kBatchSlice - 1) / kBatchSlice : (v.n + kSoloSlice - 1) / kSoloSlice);
   if (p < 1) p = 1;
   if (p > pmax) p = pmax;
   int64_t rc = (v.n + p - 1) / p;
-  if (rc > rc_cap) {
+  if (team_smem(rc, (int)p) == 0) {
     rc = (v.n + pmax - 1) / pmax;
     p = (v.n + rc - 1) / rc;
-    if (rc > rc_cap) return false;
+    if (team_smem(rc, (int)p) == 0) return false;
   }
   int pfit = 0;
-  if (team_max_blocks(team_smem(rc), &pfit) != cudaSuccess || pfit < p) {
+  if (team_max_blocks(team_smem(rc, (int)p), &pfit) != cudaSuccess || pfit < p) {
     (void)cudaGetLastError();
     return false;
   }
@@ -473,9 +475,12 @@ static int prepare_team(g4s_net *n, bool batch = false) {
     return G4S_OK;
   }
   if (!n->list) {
-    cudaError_t e = cudaMalloc((void **)&n->list, (size_t)n->v.n * 2 * sizeof(int));
+    cudaError_t e = cudaMalloc((void **)&n->list, (size_t)n->v.n * 4 * sizeof(unsigned long long));
     if (e != cudaSuccess) return cuda_error(e, "spike lists");
-    n->device_bytes += (size_t)n->v.n * 2 * sizeof(int);
+    G4S_CUDA(cudaMemsetAsync(n->list, 0, (size_t)n->v.n * 4 * sizeof(unsigned long long), n->stream));
+    G4S_CUDA(cudaStreamSynchronize(n->stream));  // a batch may launch on another handle's stream
+    n->tag_next = 0;
+    n->device_bytes += (size_t)n->v.n * 4 * sizeof(unsigned long long);
   }
   if (p > 1) {
     const size_t bytes = (size_t)n->v.n * (size_t)(p + 1) * sizeof(uint16_t);
@@ -602,7 +607,7 @@ static int team_round(g4s_net *const *nets, const int *steps, const bool *last, 
       order.push_back(i);
       nslots += nets[i]->team_p;
       maxteam = std::max(maxteam, nets[i]->team_p);
-      smem = std::max(smem, team_smem(nets[i]->team_rc));
+      smem = std::max(smem, team_smem(nets[i]->team_rc, nets[i]->team_p));
     }
   if (order.empty()) return G4S_OK;
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
@@ -620,6 +625,7 @@ static int team_round(g4s_net *const *nets, const int *steps, const bool *last, 
     it.v = n->v;
     it.seg = n->seg;
     it.list = n->list;
+    it.rec = reinterpret_cast<unsigned long long *>(n->gs + 1);
     it.t_abs0 = n->t_abs;
     it.steps = steps[i];
     it.last = last[i] ? 1 : 0;
@@ -627,11 +633,19 @@ static int team_round(g4s_net *const *nets, const int *steps, const bool *last, 
     it.rc = (int)n->team_rc;
     it.sync = n->gs;
     it.mode = n->deliver_mode;
+    it.cap = team_window(n->team_rc, n->team_p);
+    if ((uint64_t)n->tag_next + (uint64_t)steps[i] + 2 >= 0xFFFFFFFFull) {  // tags would wrap: start over
+      G4S_CUDA(cudaMemsetAsync(n->list, 0, (size_t)n->v.n * 4 * sizeof(unsigned long long), s));
+      n->tag_next = 0;
+    }
+    it.tag0 = n->tag_next;
+    n->tag_next += (uint32_t)steps[i];
     for (int r = 0; r < n->team_p; ++r) L.h_slots[k++] = make_int2(i, r);
     G4S_CUDA(cudaMemsetAsync(n->v.counts, 0, (size_t)steps[i] * sizeof(int), s));
     G4S_CUDA(cudaMemsetAsync(n->v.stamps, 0, ((size_t)steps[i] * 2 + 2) * 8, s));
     G4S_CUDA(cudaMemsetAsync(n->v.status, 0, sizeof(int), s));
-    G4S_CUDA(cudaMemsetAsync(n->gs, 0, sizeof(GridSync), s));
+    // error word and the team's spike records (two sets of kRecLines 128-byte lines per rank)
+    G4S_CUDA(cudaMemsetAsync(n->gs, 0, sizeof(GridSync) * (1 + 2 * (size_t)n->team_p * kRecLines), s));
   }
   for (int i = 0; i < count; ++i)
     if (steps[i] <= 0) L.h_items[i].steps = 0;
@@ -856,15 +870,15 @@ static int autotune(g4s_net *n, int32_t probe, TuneChoice *best, double *best_us
   const int keep_p = n->want_p;
   std::vector<TuneChoice> cand;
   int pmax = 0;
-  if (team_max_blocks(team_smem(1), &pmax) != cudaSuccess) pmax = 1;
+  if (team_max_blocks(team_smem(1, 1), &pmax) != cudaSuccess) pmax = 1;
   (void)cudaGetLastError();
+  pmax = std::min(pmax, kMaxTeam);
   std::vector<int> teams = {0};
   for (int p = 1; p <= pmax; p *= 2) teams.push_back(p);
   if (pmax > 1) teams.push_back(pmax);
-  for (int p : teams) {
-    cand.push_back(TuneChoice{kAlgSKL, p, kDeliverRun});
-    if (p != 1) cand.push_back(TuneChoice{kAlgSKL, p, kDeliverLane});
-  }
+  // segment-run delivery only: lane-per-spike measured slower or equal on every
+  // configuration tried (it stays available through g4s_net_set_geometry)
+  for (int p : teams) cand.push_back(TuneChoice{kAlgSKL, p, kDeliverRun});
   cand.push_back(TuneChoice{kAlgAB, 0, kDeliverRun});
   cand.push_back(TuneChoice{kAlgAP, 0, kDeliverRun});
   const int keep_mode = n->deliver_mode;

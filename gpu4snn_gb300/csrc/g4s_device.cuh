@@ -103,24 +103,29 @@ __device__ __forceinline__ uint4 philox32(uint32_t k0, uint32_t k1, uint32_t c0,
 // Standard normal for (neuron, step) by Marsaglia's polar method: one Philox4x32-10 call
 // (key = seed words, counter = (neuron, step, attempt, 4)) gives two candidate pairs from
 // the top 24 bits of words (0,1) and (2,3); up to 16 calls, z = 0 if all 32 pairs are
-// rejected.  Replaces curand_normal (gpu4snn.cu:358).
+// rejected.  Replaces curand_normal (gpu4snn.cu:358).  The first accepted pair is chosen
+// before the transform, so a warp runs the log / divide / square root once even when its
+// lanes accept different pairs.
 __device__ __forceinline__ float normal(uint64_t seed, uint64_t neuron, uint64_t step) {
   const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
-  for (uint32_t attempt = 0; attempt < 16; ++attempt) {
+  float x = 0.0f, s = 2.0f;
+  for (uint32_t attempt = 0; attempt < 16 && !(s < 1.0f); ++attempt) {
     const uint4 o = philox32(k0, k1, (uint32_t)neuron, (uint32_t)step, attempt, (uint32_t)kStreamNoise);
-    const uint32_t w[4] = {o.x, o.y, o.z, o.w};
-#pragma unroll
-    for (int p = 0; p < 2; ++p) {
-      const float x = pm1_from24(w[2 * p] >> 8);
-      const float y = pm1_from24(w[2 * p + 1] >> 8);
-      const float s = __fadd_rn(__fmul_rn(x, x), __fmul_rn(y, y));
-      if (s < 1.0f) {
-        const float q = __fdiv_rn(__fmul_rn(-2.0f, log_pos(s)), s);
-        return __fmul_rn(x, __fsqrt_rn(q));
-      }
+    const float x0 = pm1_from24(o.x >> 8), y0 = pm1_from24(o.y >> 8);
+    const float x1 = pm1_from24(o.z >> 8), y1 = pm1_from24(o.w >> 8);
+    const float s0 = __fadd_rn(__fmul_rn(x0, x0), __fmul_rn(y0, y0));
+    const float s1 = __fadd_rn(__fmul_rn(x1, x1), __fmul_rn(y1, y1));
+    if (s0 < 1.0f) {
+      x = x0;
+      s = s0;
+    } else if (s1 < 1.0f) {
+      x = x1;
+      s = s1;
     }
   }
-  return 0.0f;
+  if (!(s < 1.0f)) return 0.0f;
+  const float q = __fdiv_rn(__fmul_rn(-2.0f, log_pos(s)), s);
+  return __fmul_rn(x, __fsqrt_rn(q));
 }
 
 // Q32.32 fixed point of one weight (round to nearest even).
@@ -185,6 +190,17 @@ __device__ __forceinline__ float4 ld_stream_f4(const float4 *p, uint64_t pol) {
                : "l"(p), "l"(pol));
   return r;
 }
+// The per-row segment table is small and read for every spike: keep it in L2.
+__device__ __forceinline__ uint64_t policy_evict_last() {
+  uint64_t pol;
+  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
+  return pol;
+}
+__device__ __forceinline__ int ld_keep_u16(const uint16_t *p, uint64_t pol) {
+  unsigned short r;
+  asm volatile("ld.global.nc.L2::cache_hint.u16 %0, [%1], %2;" : "=h"(r) : "l"(p), "l"(pol));
+  return r;
+}
 // Fire-and-forget 64-bit integer reduction in L2 (exact, order independent).
 __device__ __forceinline__ void red_add(long long *p, long long v) {
   asm volatile("red.relaxed.gpu.global.add.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
@@ -205,6 +221,21 @@ __device__ __forceinline__ int ld_relaxed(const int *p) {
   int v;
   asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
+}
+// Spike records: 64-bit words (tag << 32 | payload), each single-copy atomic, so a reader
+// that sees the tag it expects also sees the payload written with it.
+__device__ __forceinline__ void st_relaxed_u64(unsigned long long *p, unsigned long long x) {
+  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(x) : "memory");
+}
+__device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long *p) {
+  unsigned long long r;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(r) : "l"(p) : "memory");
+  return r;
+}
+__device__ __forceinline__ ulonglong2 ld_relaxed_u64x2(const unsigned long long *p) {
+  ulonglong2 r;
+  asm volatile("ld.relaxed.gpu.global.v2.u64 {%0,%1}, [%2];" : "=l"(r.x), "=l"(r.y) : "l"(p) : "memory");
+  return r;
 }
 __device__ __forceinline__ unsigned long long globaltimer() {
   unsigned long long t;

@@ -37,9 +37,74 @@ int persistent_blocks();
 constexpr int kMaxSortedNsyn = 16384;          // rows are sorted in shared memory
 constexpr size_t kTeamSmemLimit = 200 * 1024;  // shared memory per CTA for currents + spikes
 constexpr int64_t kPrezSlice = 12288;          // slices up to this size precompute the next drive
+constexpr int64_t kVuSlice = 2048;             // ... keep v, u in shared memory for the whole launch
+constexpr int64_t kAbcdSlice = 2048;           // ... keep a, b, c, d in shared memory (larger slices
+                                               // keep them in global memory: the L1 left by a larger
+                                               // shared-memory carve-out holds fewer table loads in flight)
 constexpr int64_t kSoloSlice = 2048;           // neurons per CTA of a network running alone
 constexpr int64_t kBatchSlice = 2048;          // neurons per CTA of a batched network (measured: fewer,
                                                // larger slices made the config-4 ensemble 1.4x slower)
+constexpr int kMaxTeam = 192;                  // CTAs of one team (three record slots per thread)
+constexpr int kMinWindow = 1024;               // spike ids a multi-CTA rank can stage per delivery window
+constexpr int kMaxWindow = 4096;
+// Spike records of a multi-CTA team: per rank and step parity kRecLines lines of 16
+// tagged 64-bit words (count, then up to 16 kRecLines - 1 ids); readers fetch the second
+// line of a rank only if it had more than 15 spikes in the previous step.
+constexpr int kRecLines = 2;
+constexpr int kRecWords = 16;
+
+// Shared-memory layout of one team rank (byte offsets; the optional arrays are present
+// when their flag is set).  `cap` is the delivery window of a multi-CTA team (0 for one CTA).
+struct TeamLayout {
+  unsigned abcd, vu, a, b, own, z, cnt, off, xoff, inl, pay, spk, bytes;
+  bool abcd_sm, vu_sm, prez;
+};
+__host__ __device__ inline unsigned team_align16(size_t x) { return (unsigned)((x + 15) & ~(size_t)15); }
+__host__ __device__ inline TeamLayout team_layout(int64_t rc, int team, int cap) {
+  TeamLayout L{};
+  L.abcd_sm = rc <= kAbcdSlice;
+  L.vu_sm = rc <= kVuSlice;
+  L.prez = rc <= kPrezSlice;
+  size_t o = 0;
+  L.abcd = (unsigned)o;
+  if (L.abcd_sm) o += (size_t)rc * 16;
+  L.vu = (unsigned)o;
+  if (L.vu_sm) o += (size_t)rc * 8;
+  L.a = (unsigned)o;
+  o = team_align16(o + (size_t)rc * 4);
+  L.b = (unsigned)o;
+  o = team_align16(o + (size_t)rc * 4);
+  L.own = (unsigned)o;
+  o = team_align16(o + (size_t)rc * 4);
+  L.z = (unsigned)o;
+  if (L.prez) o = team_align16(o + (size_t)rc * 4);
+  L.cnt = L.off = L.xoff = L.inl = L.pay = L.spk = (unsigned)o;
+  if (team > 1) {
+    L.cnt = (unsigned)o;  // spikes per rank
+    o = team_align16(o + (size_t)(team + 1) * 4);
+    L.off = (unsigned)o;  // their offsets in the step's list
+    o = team_align16(o + (size_t)(team + 1) * 4);
+    L.xoff = (unsigned)o;  // offsets of the ids not in the lines read by the first pass
+    o = team_align16(o + (size_t)(team + 1) * 4);
+    L.inl = (unsigned)o;  // ids of each rank in the lines read by the first pass
+    o = team_align16(o + (size_t)(team + 1) * 4);
+    L.pay = (unsigned)o;  // payloads of the record lines
+    o = team_align16(o + (size_t)team * kRecLines * kRecWords * 4);
+    L.spk = (unsigned)o;  // the delivery window: spike ids of the step
+    o = team_align16(o + (size_t)cap * 4);
+  }
+  L.bytes = (unsigned)o;
+  return L;
+}
+// Delivery window of a multi-CTA rank: what is left of the shared-memory limit, at most
+// kMaxWindow ids; 0 if less than kMinWindow is left (the geometry does not fit).
+inline int team_window(int64_t rc, int team) {
+  if (team <= 1) return 0;
+  const size_t base = team_layout(rc, team, 0).bytes;
+  if (base + (size_t)kMinWindow * 4 > kTeamSmemLimit) return 0;
+  const size_t cap = (kTeamSmemLimit - base) / 4;
+  return (int)(cap > (size_t)kMaxWindow ? kMaxWindow : cap & ~(size_t)3);
+}
 cudaError_t launch_sort_rows(const NetView &v, cudaStream_t s);
 cudaError_t launch_segoff(const NetView &v, int team, int64_t rc, uint16_t *seg, cudaStream_t s);
 cudaError_t launch_inbound(const NetView &v, unsigned *cnt, unsigned long long *mag, unsigned long long *out,
@@ -47,7 +112,8 @@ cudaError_t launch_inbound(const NetView &v, unsigned *cnt, unsigned long long *
 cudaError_t launch_team(const TeamItem *items, const int2 *slots, const int *nslots, int *slot_head, int grid,
                         size_t smem, unsigned long long limit_ns, int stall, cudaStream_t s);
 cudaError_t team_max_blocks(size_t smem, int *out);
-size_t team_smem(int64_t rc);
+// shared memory of one rank of a team of `team` CTAs with `rc` neurons each (0: does not fit)
+size_t team_smem(int64_t rc, int team);
 
 // Error reporting (thread-local message behind g4s_last_error()).
 int set_error(int code, const std::string &msg);

@@ -6,10 +6,11 @@
 // real-time loops that must not pay the device-wide synchronisation an allocation may
 // imply, and hosts whose device memory is owned by a capped pool that this library cannot
 // draw from.  For them this entry point uses only memory it already has: the caller
-// passes the network's arrays and the output buffers, and the kernel's scratch (per-step
-// spike lists, the per-row segment table of a multi-CTA team, the team barrier and the
-// work-queue words) lives in one file-scope __device__ array of fixed size, which every
-// GPU that loads the library holds until the process exits.
+// passes the network's arrays and the output buffers, and the kernel's scratch (the
+// team's per-step spike records and overflow ids, the per-row segment table of a
+// multi-CTA team, the error word and the work-queue words) lives in one file-scope
+// __device__ array of fixed size, which every GPU that loads the library holds until
+// the process exits.
 //
 // Limits: at most kNoAllocMaxNeurons neurons and kNoAllocMaxTeam CTAs, and at most 16384
 // neurons per CTA (the shared-memory slice of the team kernel).  Every call shares the
@@ -34,21 +35,22 @@ constexpr int kNoAllocMaxTeam = 8;
 constexpr int64_t kNoAllocMaxSlice = 16384;
 
 // Layout of the scratch array.
-constexpr size_t kOffSync = 0;                                  // GridSync (128 B)
-constexpr size_t kOffCtl = 128;                                 // int[4]: slot count, queue head, status
-constexpr size_t kOffSlots = 256;                               // int2[kNoAllocMaxTeam]
-constexpr size_t kOffItem = 512;                                // TeamItem
-constexpr size_t kOffList = 4096;                               // int[2][kNoAllocMaxNeurons]
-constexpr size_t kOffSeg = kOffList + 2 * kNoAllocMaxNeurons * 4;  // u16[kNoAllocMaxNeurons][kNoAllocMaxTeam + 1]
+constexpr size_t kOffSync = 0;                                       // GridSync (128 B): error word
+constexpr size_t kOffRec = 128;                                      // spike records: [2][team][4 x 16] u64
+constexpr size_t kOffCtl = kOffRec + 2 * kNoAllocMaxTeam * kRecLines * 128;  // int[4]: slot count, queue head, status
+constexpr size_t kOffSlots = kOffCtl + 128;                          // int2[kNoAllocMaxTeam]
+constexpr size_t kOffItem = kOffSlots + 256;                         // TeamItem
+constexpr size_t kOffList = 16384;                                   // u64[4][kNoAllocMaxNeurons]: overflow, dense ids
+constexpr size_t kOffSeg = kOffList + 4 * kNoAllocMaxNeurons * 8;  // u16[kNoAllocMaxNeurons][kNoAllocMaxTeam + 1]
 constexpr size_t kScratchBytes = kOffSeg + (size_t)kNoAllocMaxNeurons * (kNoAllocMaxTeam + 1) * 2;
 
-static_assert(sizeof(GridSync) <= kOffCtl - kOffSync, "barrier word");
+static_assert(sizeof(GridSync) <= kOffRec - kOffSync, "error word");
 static_assert(sizeof(int2) * kNoAllocMaxTeam <= kOffItem - kOffSlots, "slots");
 static_assert(sizeof(TeamItem) <= kOffList - kOffItem, "item");
 
 }  // namespace
 
-// The scratch of g4s_run_noalloc (about 3.4 MB per GPU, held until exit).
+// The scratch of g4s_run_noalloc (about 6.5 MB per GPU, held until exit).
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
 // In host code g_noalloc_scratch names a host-side stand-in, not device memory: its
@@ -83,7 +85,7 @@ extern "C" int g4s_run_noalloc(const g4s_dev_net *d, int64_t t_abs0, int32_t ste
     return set_error(G4S_ERR_INVALID, "g4s_run_noalloc: team must be in [1, " + std::to_string(kNoAllocMaxTeam) +
                                           "], got " + std::to_string(team));
   const int64_t rc = (d->n + team - 1) / team;
-  if (rc > kNoAllocMaxSlice)
+  if (rc > kNoAllocMaxSlice || team_smem(rc, team) == 0)
     return set_error(G4S_ERR_INVALID, "g4s_run_noalloc: more than " + std::to_string(kNoAllocMaxSlice) +
                                           " neurons per CTA; use a larger team");
   if (d->nsyn < 1 || d->stride < d->nsyn || d->stride % 4 != 0 || d->stride > kMaxSortedNsyn)
@@ -106,7 +108,7 @@ extern "C" int g4s_run_noalloc(const g4s_dev_net *d, int64_t t_abs0, int32_t ste
   int *ctl = reinterpret_cast<int *>(scr + kOffCtl);
   int2 *slots = reinterpret_cast<int2 *>(scr + kOffSlots);
   TeamItem *item = reinterpret_cast<TeamItem *>(scr + kOffItem);
-  int *list = reinterpret_cast<int *>(scr + kOffList);
+  unsigned long long *list = reinterpret_cast<unsigned long long *>(scr + kOffList);
   uint16_t *seg = reinterpret_cast<uint16_t *>(scr + kOffSeg);
 
   TeamItem h{};
@@ -133,6 +135,9 @@ extern "C" int g4s_run_noalloc(const g4s_dev_net *d, int64_t t_abs0, int32_t ste
   v.status = ctl + 2;
   h.seg = seg;
   h.list = list;
+  h.rec = reinterpret_cast<unsigned long long *>(scr + kOffRec);
+  h.cap = team_window(rc, team);
+  h.tag0 = 0;
   h.t_abs0 = t_abs0;
   h.steps = steps;
   h.last = last ? 1 : 0;
@@ -143,15 +148,17 @@ extern "C" int g4s_run_noalloc(const g4s_dev_net *d, int64_t t_abs0, int32_t ste
   for (int r = 0; r < team; ++r) hs[r] = make_int2(0, r);
   const int hc[2] = {team, 0};
 
-  // Everything that must start at zero: barrier and error word, queue head, step counts.
+  // Everything that must start at zero: error word, spike records and overflow ids (their
+  // tags restart with every call), queue head, step counts.
   cudaError_t e = cudaMemsetAsync(scr, 0, kOffSlots, s);
+  if (e == cudaSuccess && team > 1) e = cudaMemsetAsync(list, 0, (size_t)d->n * 4 * sizeof(unsigned long long), s);
   if (e == cudaSuccess) e = cudaMemsetAsync(d_counts, 0, (size_t)steps * sizeof(int32_t), s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(ctl, hc, sizeof hc, cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(slots, hs, sizeof(int2) * team, cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(item, &h, sizeof h, cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess && team > 1) e = launch_segoff(v, team, rc, seg, s);
   if (e == cudaSuccess)
-    e = launch_team(item, slots, ctl, ctl + 1, team, team_smem(rc), 2000000000ull, 0, s);
+    e = launch_team(item, slots, ctl, ctl + 1, team, team_smem(rc, team), 2000000000ull, 0, s);
   if (e == cudaSuccess && d_status) e = cudaMemcpyAsync(d_status, &sync->error, sizeof(int32_t), cudaMemcpyDeviceToDevice, s);
   if (e != cudaSuccess) return cuda_error(e, "g4s_run_noalloc launch");
   return G4S_OK;

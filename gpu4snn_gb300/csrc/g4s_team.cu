@@ -16,23 +16,35 @@
 // about five times faster than 64-bit ones on this part, and the split is exact as long
 // as no neuron has 65536 or more incoming synapses and the sum of |q_i| / 2^16 + 1 over
 // its incoming synapses stays below 2^31; k_inbound checks both once per table (the
-// host falls back to the global-atomic persistent kernel otherwise).
+// host falls back to the global-atomic persistent kernel otherwise).  Small slices also
+// keep v, u (and a, b, c, d) in shared memory for the launch.
 //
 // Per step, for each team:
 //   update    every rank updates its own neurons (current read from and cleared in shared
 //             memory; drive precomputed in shared memory during the previous step) and
 //             collects its spikes in shared memory;
 //   exchange  one-CTA team: nothing, the spike list stays in shared memory.  Larger team:
-//             each rank appends its spikes to the network's global list of the step (two
-//             lists, by step parity), then a team barrier with a bounded spin;
+//             each rank publishes its spike count and ids as 64-bit words, each tagged
+//             with a step number that never repeats for the network's buffers, so a
+//             reader that sees the tag it expects needs no fence to trust the payload:
+//             two 128-byte record lines (count and 31 ids), further ids in a per-rank
+//             overflow list.  Every rank reads, in one pass, line 0 of every rank and
+//             line 1 of the ranks that had more than 15 spikes in the previous step
+//             (16-byte slots, polled until their tags are current, with a time limit), so
+//             the records double as the team barrier; ids beyond the lines read are
+//             polled word by word.  The step's ids are staged in shared memory (in
+//             windows when they do not fit).  Records are cleared before each launch.
+//             Two record sets (by step parity) suffice: a rank writes step t+2's words
+//             only after every rank has published step t+1, i.e. finished reading step t.
 //   delivery  one-CTA team: whole spiking rows, 128-bit loads, flat over all threads.
 //             Larger team: every rank streams, for every spike, the segment of the
 //             spiking row whose targets fall in its slice (rows are sorted by target and
 //             a per-row offset table gives the segment): a warp takes 32 spikes, scans
 //             their segment lengths and walks the concatenated segments, eight synapses
 //             per lane in flight.  Each weight goes into the rank's own shared memory.
-//   tail      once its delivery share is done, each thread updates the spike statistics
-//             of this CTA's spikes and computes the next step's drive of its neurons.
+//   tail      the raster and the spike statistics of this rank's spikes, and the next
+//             step's drive, handed out in chunks of 32 neurons to warps as they finish
+//             delivering.
 //   The raster records the spike ids of every step while its buffer has room.
 #include <cuda_runtime.h>
 
@@ -143,20 +155,78 @@ __device__ __forceinline__ void acc_add4(unsigned base_a, unsigned base_b, int l
   if (t.w >= 0) acc_add(base_a, base_b, (unsigned)(t.w - lo), wfix(w.w));
 }
 
+// Last index r in [0, n) with a[r] <= x, for a non-decreasing a[0..n] with a[0] <= x < a[n].
+__device__ __forceinline__ int find_run(const int *a, int n, int x) {
+  int lo = 0, hi = n;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (a[mid] <= x)
+      lo = mid;
+    else
+      hi = mid;
+  }
+  return lo;
+}
+
+// Scalars of one CTA shared by the phases of a step; the per-step counters come in pairs
+// (by step parity) so that one is cleared while the other is in use.
+struct TeamShared {
+  int nown[2];  // spikes of this rank in the step
+  int work[2];  // next chunk of the next step's drive
+  int fail;     // the exchange gave up (time limit, or the team's error word was set)
+  int slot;     // queue slot taken by this CTA
+};
+
+// Record words of a rank per step: word 0 = spike count, words 1.. = ids (kInline inline);
+// a thread reads up to kSlots 16-byte slots of a step's records.
+constexpr int kRankWords = kRecLines * kRecWords;
+constexpr int kInline = kRankWords - 1;
+constexpr int kSlots = (kMaxTeam * kRankWords / 2 + 1023) / 1024;
+constexpr int kLine1After = 7;  // line 1 of a rank is read if it had more spikes in the previous step
+
+// Gives up a wait: first error wins, every CTA of the team leaves at its next check.
+__device__ __forceinline__ void give_up(TeamShared &sh, GridSync *gs) {
+  atomicCAS(&gs->error, 0, kErrTimeoutCode);
+  *(volatile int *)&sh.fail = 1;
+}
+
+// One tagged word of another rank, polled until it carries `tag` (or the time limit).
+__device__ __forceinline__ int tagged_id(const unsigned long long *p, unsigned tag, TeamShared &sh, GridSync *gs,
+                                         unsigned long long lim) {
+  unsigned long long w = ld_relaxed_u64(p);
+  if ((unsigned)(w >> 32) == tag) return (int)(unsigned)w;
+  const unsigned long long t0 = globaltimer();
+  for (;;) {
+    w = ld_relaxed_u64(p);
+    if ((unsigned)(w >> 32) == tag) return (int)(unsigned)w;
+    if (*(volatile int *)&sh.fail || ld_relaxed(&gs->error) != 0 || globaltimer() - t0 > lim) {
+      give_up(sh, gs);
+      return 0;
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------------------
 // One team member's share of one network for the steps of this launch.
 // ---------------------------------------------------------------------------------------
 template <int NT>
-__device__ void team_run(const TeamItem &it, int rank, unsigned char *s_raw, int *s_nspk, long long *s_gpos,
+__device__ void team_run(const TeamItem &it, int rank, unsigned char *s_raw, TeamShared &sh,
                          unsigned long long limit_ns, int stall) {
   const NetView &v = it.v;
   const int T = it.team, rc = it.rc;
-  int *s_a = reinterpret_cast<int *>(s_raw);
-  unsigned *s_b = reinterpret_cast<unsigned *>(s_raw + (size_t)rc * 4);
-  int *s_spk = reinterpret_cast<int *>(s_raw + (size_t)rc * 8);
-  // drive of the next step, computed during this step's delivery (slices up to kPrezSlice)
-  float *s_z = reinterpret_cast<float *>(s_raw + (size_t)rc * 12);
-  const bool prez = rc <= kPrezSlice;
+  const TeamLayout L = team_layout(rc, T, it.cap);
+  float4 *s_abcd = reinterpret_cast<float4 *>(s_raw + L.abcd);
+  float2 *s_vu = reinterpret_cast<float2 *>(s_raw + L.vu);
+  int *s_a = reinterpret_cast<int *>(s_raw + L.a);
+  unsigned *s_b = reinterpret_cast<unsigned *>(s_raw + L.b);
+  int *s_own = reinterpret_cast<int *>(s_raw + L.own);
+  float *s_z = reinterpret_cast<float *>(s_raw + L.z);
+  int *s_cnt = reinterpret_cast<int *>(s_raw + L.cnt);
+  int *s_off = reinterpret_cast<int *>(s_raw + L.off);
+  int *s_xoff = reinterpret_cast<int *>(s_raw + L.xoff);
+  int *s_inl = reinterpret_cast<int *>(s_raw + L.inl);
+  unsigned *s_pay = reinterpret_cast<unsigned *>(s_raw + L.pay);
+  int *s_spk = reinterpret_cast<int *>(s_raw + L.spk);
   const int64_t lo = min((int64_t)rank * rc, v.n);
   const int64_t hi = min(lo + rc, v.n);
   const int cnt = (int)(hi - lo);
@@ -165,23 +235,37 @@ __device__ void team_run(const TeamItem &it, int rank, unsigned char *s_raw, int
   const unsigned segw = (unsigned)T + 1;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   constexpr int kWarps = NT / 32;
-  const bool shared_list = T == 1 && stall == 0;  // the whole network in this CTA
-  const unsigned nb = (unsigned)T + (unsigned)stall;  // stall > 0 only under fault injection
+  const bool solo = T == 1;   // the whole network in this CTA: no exchange
   const bool lead = rank == 0 && threadIdx.x == 0;
+  // neuron state of the slice: shared memory for the launch when it fits, else global
+  float2 *vu = L.vu_sm ? s_vu : v.vu + lo;
+  const float4 *abcd = L.abcd_sm ? s_abcd : v.abcd + lo;
 
   for (int i = threadIdx.x; i < cnt; i += NT) {
     const long long q = __ldcg(v.acc + lo + i);
     s_a[i] = (int)(q >> 16);
     s_b[i] = (unsigned)(q & 0xFFFF);
+    if (L.vu_sm) s_vu[i] = v.vu[lo + i];
+    if (L.abcd_sm) s_abcd[i] = v.abcd[lo + i];
   }
-  if (threadIdx.x == 0) *s_nspk = 0;
+  if (!solo)  // the first step reads one record line per rank
+    for (int r = threadIdx.x; r <= T; r += NT) s_cnt[r] = 0;
+  if (threadIdx.x == 0) {
+    sh.nown[0] = sh.nown[1] = 0;
+    sh.work[0] = sh.work[1] = 0;
+    sh.fail = 0;
+  }
   __syncthreads();
 
-  unsigned epoch = 0;
   long long base = 0;
   for (int lt = 0; lt < it.steps; ++lt) {
     const int64_t t_abs = it.t_abs0 + lt;
     const bool last = it.last && lt == it.steps - 1;
+    const int par = lt & 1;
+    if (threadIdx.x == 0) {
+      sh.nown[par ^ 1] = 0;  // last used by the previous step, next by the following one
+      sh.work[par ^ 1] = 0;
+    }
     if (lead) {
       v.base[lt] = base;
       if (v.stamps) v.stamps[2 * lt] = globaltimer();
@@ -190,9 +274,10 @@ __device__ void team_run(const TeamItem &it, int rank, unsigned char *s_raw, int
     for (int i0 = threadIdx.x; i0 < cnt; i0 += 2 * NT) {
       const int i1 = i0 + NT;
       const bool h1 = i1 < cnt;
-      const int64_t n0 = lo + i0, n1 = lo + (h1 ? i1 : i0);
-      float2 s0 = v.vu[n0], s1 = v.vu[n1];
-      const float4 p0 = v.abcd[n0], p1 = v.abcd[n1];
+      const int j1 = h1 ? i1 : i0;
+      const int64_t n0 = lo + i0, n1 = lo + j1;
+      float2 s0 = vu[i0], s1 = vu[j1];
+      const float4 p0 = abcd[i0], p1 = abcd[j1];
       const long long a0 = (long long)s_a[i0] * 65536 + s_b[i0];
       const long long a1 = h1 ? (long long)s_a[i1] * 65536 + s_b[i1] : 0;
       s_a[i0] = 0;
@@ -201,179 +286,325 @@ __device__ void team_run(const TeamItem &it, int rank, unsigned char *s_raw, int
         s_a[i1] = 0;
         s_b[i1] = 0;
       }
-      const bool use_z = prez && lt > 0;
+      const bool use_z = L.prez && lt > 0;
       const float z0 = use_z ? s_z[i0] : normal(v.seed, (uint64_t)n0, (uint64_t)t_abs);
       const float z1 = use_z ? (h1 ? s_z[i1] : 0.0f) : normal(v.seed, (uint64_t)n1, (uint64_t)t_abs);
       float I0, I1;
       const bool k0 = izh_step(s0.x, s0.y, I0, p0, n0 < v.nexc ? v.ge : v.gi, z0, a0);
       const bool k1 = izh_step(s1.x, s1.y, I1, p1, n1 < v.nexc ? v.ge : v.gi, z1, a1) && h1;
-      v.vu[n0] = s0;
-      if (h1) v.vu[n1] = s1;
+      vu[i0] = s0;
+      if (h1) vu[i1] = s1;
       if (last) {
         v.ilast[n0] = I0;
         if (h1) v.ilast[n1] = I1;
       }
-      if (k0) s_spk[atomicAdd(s_nspk, 1)] = (int)n0;
-      if (k1) s_spk[atomicAdd(s_nspk, 1)] = (int)n1;
+      if (k0) s_own[atomicAdd(&sh.nown[par], 1)] = (int)n0;
+      if (k1) s_own[atomicAdd(&sh.nown[par], 1)] = (int)n1;
     }
     __syncthreads();
-    const int nspk = *s_nspk;
-    if (threadIdx.x == 0) *s_gpos = shared_list ? 0 : (nspk ? atomicAdd(v.counts + lt, nspk) : 0);
-    __syncthreads();
-    if (threadIdx.x == 0) *s_nspk = 0;
-    int *glist = it.list + (size_t)(lt & 1) * (size_t)v.n;
-    for (int j = threadIdx.x; j < nspk; j += NT) {
-      const int id = s_spk[j];
-      const long long pos = base + *s_gpos + j;
-      if (!shared_list) glist[*s_gpos + j] = id;
-      if (pos < v.raster_cap) v.raster[pos] = id;
-    }
-    int K = nspk;
-    if (shared_list) {
-      if (threadIdx.x == 0) v.counts[lt] = nspk;
-    } else {
-      // ---- the step's spike list is complete for the whole team after this barrier
-      if (!grid_barrier(it.sync, nb, epoch, epoch == 0 ? limit_ns * 16 : limit_ns)) return;
-      K = __ldcg(v.counts + lt);
-    }
-    if (lead && v.stamps) v.stamps[2 * lt + 1] = globaltimer();
-    if (shared_list) {
-      // ---- delivery, one-CTA team: flat over K whole rows of stride/4 vectors
-      const int rv = v.stride >> 2;
-      const int total = K * rv;
-      const int dq = NT / rv, dj = NT - dq * rv;
-      int q = threadIdx.x / rv, j = threadIdx.x - q * rv;
-      const int4 *ti = reinterpret_cast<const int4 *>(v.idx);
-      const float4 *wi = reinterpret_cast<const float4 *>(v.w);
-      const uint64_t pol = policy_evict_first();
-      for (int g = threadIdx.x; g < total; g += 2 * NT) {
-        const size_t o0 = (size_t)s_spk[q] * rv + j;
-        int q1 = q + dq, j1 = j + dj;
-        if (j1 >= rv) {
-          j1 -= rv;
-          q1 += 1;
+    const int nown = sh.nown[par];
+    const unsigned long long lim = lt == 0 ? limit_ns * 16 : limit_ns;  // members may start late
+    if (stall != 0 && solo) {
+      // injected fault of a one-CTA team: wait for a member that does not exist
+      if (threadIdx.x == 0) {
+        const unsigned long long t0 = globaltimer();
+        while (ld_relaxed(&it.sync->error) == 0 && globaltimer() - t0 <= lim) {
         }
-        const bool h1 = g + NT < total;
-        const size_t o1 = h1 ? (size_t)s_spk[q1] * rv + j1 : o0;
-        const int4 t0 = ld_stream_i4(ti + o0, pol), t1 = ld_stream_i4(ti + o1, pol);
-        const float4 w0 = ld_stream_f4(wi + o0, pol), w1 = ld_stream_f4(wi + o1, pol);
-        acc_add4(base_a, base_b, 0, t0, w0);
-        if (h1) acc_add4(base_a, base_b, 0, t1, w1);
-        q = q1 + dq;
-        j = j1 + dj;
-        if (j >= rv) {
-          j -= rv;
-          q += 1;
+        give_up(sh, it.sync);
+      }
+      __syncthreads();
+      return;
+    }
+    int K = nown, my_off = 0;
+    const int *list = s_own;
+    const unsigned tag = it.tag0 + (unsigned)lt + 1u;
+    const unsigned long long *recs = it.rec + (size_t)par * T * kRankWords;
+    const unsigned long long *ovf_all = it.list + (size_t)par * v.n;
+    unsigned long long *dense = it.list + (size_t)(2 + par) * v.n;
+    bool gl = false;  // the step's ids are read from the dense list in global memory
+    if (!solo) {
+      // ---- publish: both record lines of this rank (count, ids, padding), ids beyond
+      // them in the overflow list; every word tagged with the step, so no fence is needed
+      {
+        const unsigned long long tg = (unsigned long long)tag << 32;
+        unsigned long long *ovf = it.list + (size_t)par * v.n + lo;
+        for (int j = kInline + threadIdx.x; j < nown; j += NT) st_relaxed_u64(ovf + j, tg | (unsigned)s_own[j]);
+        if (threadIdx.x < kRankWords) {
+          const int j = threadIdx.x;
+          const unsigned pay = j == 0 ? (unsigned)nown : (j - 1 < nown ? (unsigned)s_own[j - 1] : 0xFFFFFFFFu);
+          st_relaxed_u64(it.rec + ((size_t)par * T + rank) * kRankWords + j, tg | pay);
         }
       }
-    } else if (it.mode == kDeliverLane) {
-      // ---- delivery, larger team, one lane per spike: each lane walks its own segment,
-      // four synapses (eight loads) at a time; the warp's next 32 spike ids and segment
-      // bounds are loaded while the current ones are walked.  No shuffles: the shared-
-      // memory pipe carries only the atomics.
-      int q = warp * 32 + lane;
-      int s = 0, b = 0, e = 0;
-      if (q < K) {
-        s = __ldcg(glist + q);
-        const uint16_t *so = it.seg + (size_t)s * segw + rank;
-        b = so[0];
-        e = so[1];
-      }
-      for (int q0 = warp * 32; q0 < K; q0 += kWarps * 32) {
-        const int *ri = v.idx + (size_t)s * v.stride;
-        const float *rw = v.w + (size_t)s * v.stride;
-        const int cb = b, ce = e;
-        q = q0 + kWarps * 32 + lane;
-        s = 0;
-        b = 0;
-        e = 0;
-        if (q < K) {
-          s = __ldcg(glist + q);
-          const uint16_t *so = it.seg + (size_t)s * segw + rank;
-          b = so[0];
-          e = so[1];
-        }
-        for (int j = cb; j < ce; j += 4) {
-          int t[4];
-          float w[4];
+      // ---- first pass: line 0 of every rank and line 1 of the ranks that had more than
+      // kLine1After spikes in the previous step, as 16-byte slots (slot x = words 2x, 2x+1 of the
+      // step's records, rank x / 16), up to three per thread; each warp polls its slots
+      // until all carry the step's tag, then the payloads go to shared memory
+      unsigned need = 0;
 #pragma unroll
-          for (int u = 0; u < 4; ++u) {
-            t[u] = -1;
-            w[u] = 0.0f;
-            if (j + u < ce) {
-              t[u] = __ldg(ri + j + u);
-              w[u] = __ldg(rw + j + u);
-            }
+      for (int k = 0; k < kSlots; ++k) {
+        const int x = threadIdx.x + k * NT;
+        if (x < T * 16 && ((x & 15) < 8 || s_cnt[x >> 4] > kLine1After)) need |= 1u << k;
+      }
+      unsigned long long t0 = 0;
+      for (int iter = 0;; ++iter) {
+        ulonglong2 a[kSlots];
+#pragma unroll
+        for (int k = 0; k < kSlots; ++k)
+          if (need & (1u << k)) a[k] = ld_relaxed_u64x2(recs + 2 * (threadIdx.x + k * NT));
+#pragma unroll
+        for (int k = 0; k < kSlots; ++k)
+          if ((need & (1u << k)) && (unsigned)(a[k].x >> 32) == tag && (unsigned)(a[k].y >> 32) == tag) {
+            const int x = threadIdx.x + k * NT;
+            s_pay[2 * x] = (unsigned)a[k].x;
+            s_pay[2 * x + 1] = (unsigned)a[k].y;
+            need &= ~(1u << k);
           }
-#pragma unroll
-          for (int u = 0; u < 4; ++u)
-            if (t[u] >= 0) acc_add(base_a, base_b, (unsigned)(t[u] - (int)lo), wfix(w[u]));
+        if (__all_sync(0xFFFFFFFFu, need == 0) && stall == 0) break;
+        int f = 0;
+        if (lane == 0) {
+          const unsigned long long now = globaltimer();
+          if (iter == 0) t0 = now;
+          f = *(volatile int *)&sh.fail;
+          if (!f && warp == 0 && ld_relaxed(&it.sync->error) != 0) f = 1;
+          if (!f && now - t0 > lim) {
+            give_up(sh, it.sync);
+            f = 1;
+          }
+          if (f) *(volatile int *)&sh.fail = 1;
         }
+        if (__shfl_sync(0xFFFFFFFFu, f, 0)) break;
       }
-    } else {
-      // ---- delivery, larger team: this rank's segment of every spiking row.  Spikes go
-      // to warps in batches of 32; when there are fewer batches than warps, `wpb` warps
-      // share a batch and split its run.  The next batch's spike ids and segment bounds
-      // are loaded before the current run is walked.
-      const int nbatch = (K + 31) >> 5;
-      const int wpb = nbatch >= kWarps ? 1 : kWarps / max(nbatch, 1);
-      const int groups = kWarps / wpb, gw = warp / wpb, wi = warp % wpb;
-      int s = 0, b = 0, len = 0;
-      auto fetch = [&](int batch) {
-        const int q = batch * 32 + lane;
-        s = 0;
-        b = 0;
-        len = 0;
-        if (gw < groups && batch < nbatch && q < K) {
-          s = __ldcg(glist + q);
-          const uint16_t *so = it.seg + (size_t)s * segw + rank;
-          b = so[0];
-          len = (int)so[1] - b;
+      __syncthreads();
+      if (sh.fail) return;
+      if (warp == 0) {
+        // per rank: count, ids in the lines read (15 or 31), offsets of all ids and of
+        // those beyond the lines read
+        constexpr int kPer = kMaxTeam / 32;
+        int c[kPer], xr[kPer], sc = 0, sx = 0;
+#pragma unroll
+        for (int k = 0; k < kPer; ++k) {
+          const int r = lane * kPer + k;
+          c[k] = 0;
+          xr[k] = 0;
+          if (r < T) {
+            const int inl = s_cnt[r] > kLine1After ? kInline : kRecWords - 1;
+            c[k] = (int)s_pay[r * kRankWords];
+            xr[k] = max(0, c[k] - inl);
+            s_inl[r] = inl;
+          }
+          sc += c[k];
+          sx += xr[k];
         }
-      };
-      fetch(gw);
-      for (int batch = gw; gw < groups && batch < nbatch; batch += groups) {
-        int incl = len;
+        int ic = sc, ix = sx;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-          const int y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-          if (lane >= o) incl += y;
+          const int yc = __shfl_up_sync(0xFFFFFFFFu, ic, o), yx = __shfl_up_sync(0xFFFFFFFFu, ix, o);
+          if (lane >= o) {
+            ic += yc;
+            ix += yx;
+          }
         }
-        const int total = __shfl_sync(0xFFFFFFFFu, incl, 31);
-        const int excl = incl - len;
-        const long long rowoff = (long long)s * v.stride + b - excl;  // synapse f of the run: rowoff_j + f
-        fetch(batch + groups);                                        // next batch, in flight meanwhile
-        for (int f0 = wi * 256; f0 < total; f0 += wpb * 256) {
-          int t[8];
-          float w[8];
+        int ec = ic - sc, ex = ix - sx;
 #pragma unroll
-          for (int u = 0; u < 8; ++u) {
-            const int f = f0 + u * 32 + lane;
-            // spike j of the run holding f: last lane whose exclusive prefix is <= f
-            int jj = 0;
+        for (int k = 0; k < kPer; ++k) {
+          const int r = lane * kPer + k;
+          if (r < T) {
+            s_cnt[r] = c[k];
+            s_off[r] = ec;
+            s_xoff[r] = ex;
+          }
+          ec += c[k];
+          ex += xr[k];
+        }
+        if (lane == 31) {
+          s_off[T] = ec;
+          s_xoff[T] = ex;
+        }
+      }
+      __syncthreads();
+      K = s_off[T];
+      my_off = s_off[rank];
+      list = s_spk;
+      if (K > it.cap) {
+        // many spikes: instead of staging windows, every rank writes its ids (tagged) at
+        // its offset in the step's dense list, which the delivery reads directly
+        gl = true;
+        const unsigned long long tg = (unsigned long long)tag << 32;
+        for (int j = threadIdx.x; j < nown; j += NT) st_relaxed_u64(dense + my_off + j, tg | (unsigned)s_own[j]);
+      }
+    }
+    if (lead && v.stamps) v.stamps[2 * lt + 1] = globaltimer();
+    if (lead) v.counts[lt] = K;
+
+    {
+      const int Kw = K;
+      if (!solo && !gl && K > 0) {
+        // ---- stage the step's spike ids in shared memory: the first pass's payloads,
+        // then ids beyond the lines read, polled from the records or the overflow list
+        {
 #pragma unroll
-            for (int step = 16; step; step >>= 1) {
-              const int e = __shfl_sync(0xFFFFFFFFu, excl, jj + step);
-              if (e <= f) jj += step;
-            }
-            const long long off = __shfl_sync(0xFFFFFFFFu, rowoff, jj) + f;
-            t[u] = -1;
-            w[u] = 0.0f;
-            if (f < total) {
-              t[u] = __ldg(v.idx + off);
-              w[u] = __ldg(v.w + off);
+          for (int k = 0; k < kSlots; ++k) {
+            const int x = threadIdx.x + k * NT;
+            if (x < T * 16) {
+              const int r = x >> 4, w0 = 2 * (x & 15), c = min(s_cnt[r], s_inl[r]), o = s_off[r] - 1;
+              if (w0 >= 1 && w0 - 1 < c) s_spk[o + w0] = (int)s_pay[2 * x];
+              if (w0 < c) s_spk[o + w0 + 1] = (int)s_pay[2 * x + 1];
             }
           }
+          const int X = s_xoff[T];
+          for (int e = threadIdx.x; e < X; e += NT) {
+            const int r = find_run(s_xoff, T, e);
+            const int j = s_inl[r] + e - s_xoff[r];
+            s_spk[s_off[r] + j] = tagged_id(
+                j < kInline ? recs + (size_t)r * kRankWords + 1 + j : ovf_all + (size_t)r * rc + j, tag, sh, it.sync, lim);
+          }
+        }
+        __syncthreads();
+        if (sh.fail) return;
+      }
+      if (solo) {
+        // ---- delivery, one-CTA team: flat over K whole rows of stride/4 vectors
+        const int rv = v.stride >> 2;
+        const int total = Kw * rv;
+        const int dq = NT / rv, dj = NT - dq * rv;
+        int q = threadIdx.x / rv, j = threadIdx.x - q * rv;
+        const int4 *ti = reinterpret_cast<const int4 *>(v.idx);
+        const float4 *wi = reinterpret_cast<const float4 *>(v.w);
+        const uint64_t pol = policy_evict_first();
+        for (int g = threadIdx.x; g < total; g += 2 * NT) {
+          const size_t o0 = (size_t)list[q] * rv + j;
+          int q1 = q + dq, j1 = j + dj;
+          if (j1 >= rv) {
+            j1 -= rv;
+            q1 += 1;
+          }
+          const bool h1 = g + NT < total;
+          const size_t o1 = h1 ? (size_t)list[q1] * rv + j1 : o0;
+          const int4 t0 = ld_stream_i4(ti + o0, pol), t1 = ld_stream_i4(ti + o1, pol);
+          const float4 w0 = ld_stream_f4(wi + o0, pol), w1 = ld_stream_f4(wi + o1, pol);
+          acc_add4(base_a, base_b, 0, t0, w0);
+          if (h1) acc_add4(base_a, base_b, 0, t1, w1);
+          q = q1 + dq;
+          j = j1 + dj;
+          if (j >= rv) {
+            j -= rv;
+            q += 1;
+          }
+        }
+      } else if (it.mode == kDeliverLane) {
+        // ---- delivery, larger team, one lane per spike: each lane walks its own segment,
+        // four synapses (eight loads) at a time; the warp's next 32 spike ids and segment
+        // bounds are loaded while the current ones are walked.  No shuffles: the shared-
+        // memory pipe carries only the atomics.
+        const uint64_t pkeep = policy_evict_last();
+        int q = warp * 32 + lane;
+        int s = 0, b = 0, e = 0;
+        if (q < Kw) {
+          s = gl ? tagged_id(dense + q, tag, sh, it.sync, lim) : list[q];
+          const uint16_t *so = it.seg + (size_t)s * segw + rank;
+          b = ld_keep_u16(so, pkeep);
+          e = ld_keep_u16(so + 1, pkeep);
+        }
+        for (int q0 = warp * 32; q0 < Kw; q0 += kWarps * 32) {
+          const int *ri = v.idx + (size_t)s * v.stride;
+          const float *rw = v.w + (size_t)s * v.stride;
+          const int cb = b, ce = e;
+          q = q0 + kWarps * 32 + lane;
+          s = 0;
+          b = 0;
+          e = 0;
+          if (q < Kw) {
+            s = gl ? tagged_id(dense + q, tag, sh, it.sync, lim) : list[q];
+            const uint16_t *so = it.seg + (size_t)s * segw + rank;
+            b = ld_keep_u16(so, pkeep);
+            e = ld_keep_u16(so + 1, pkeep);
+          }
+          for (int j = cb; j < ce; j += 4) {
+            int t[4];
+            float w[4];
 #pragma unroll
-          for (int u = 0; u < 8; ++u)
-            if (t[u] >= 0) acc_add(base_a, base_b, (unsigned)(t[u] - (int)lo), wfix(w[u]));
+            for (int u = 0; u < 4; ++u) {
+              t[u] = -1;
+              w[u] = 0.0f;
+              if (j + u < ce) {
+                t[u] = __ldg(ri + j + u);
+                w[u] = __ldg(rw + j + u);
+              }
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+              if (t[u] >= 0) acc_add(base_a, base_b, (unsigned)(t[u] - (int)lo), wfix(w[u]));
+          }
+        }
+      } else {
+        // ---- delivery, larger team: this rank's segment of every spiking row.  Spikes go
+        // to warps in batches of 32; when there are fewer batches than warps, `wpb` warps
+        // share a batch and split its run.  The next batch's spike ids and segment bounds
+        // are loaded before the current run is walked.
+        const uint64_t pkeep = policy_evict_last();
+        const int nbatch = (Kw + 31) >> 5;
+        const int wpb = nbatch >= kWarps ? 1 : kWarps / max(nbatch, 1);
+        const int groups = kWarps / wpb, gw = warp / wpb, wi = warp % wpb;
+        int s = 0, b = 0, len = 0;
+        auto fetch = [&](int batch) {
+          const int q = batch * 32 + lane;
+          s = 0;
+          b = 0;
+          len = 0;
+          if (gw < groups && batch < nbatch && q < Kw) {
+            s = gl ? tagged_id(dense + q, tag, sh, it.sync, lim) : list[q];
+            const uint16_t *so = it.seg + (size_t)s * segw + rank;
+            b = ld_keep_u16(so, pkeep);
+            len = ld_keep_u16(so + 1, pkeep) - b;
+          }
+        };
+        fetch(gw);
+        for (int batch = gw; gw < groups && batch < nbatch; batch += groups) {
+          int incl = len;
+#pragma unroll
+          for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+            if (lane >= o) incl += y;
+          }
+          const int total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+          const int excl = incl - len;
+          const long long rowoff = (long long)s * v.stride + b - excl;  // synapse f of the run: rowoff_j + f
+          fetch(batch + groups);                                        // next batch, in flight meanwhile
+          for (int f0 = wi * 256; f0 < total; f0 += wpb * 256) {
+            int t[8];
+            float w[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+              const int f = f0 + u * 32 + lane;
+              // spike j of the run holding f: last lane whose exclusive prefix is <= f
+              int jj = 0;
+#pragma unroll
+              for (int step = 16; step; step >>= 1) {
+                const int e = __shfl_sync(0xFFFFFFFFu, excl, jj + step);
+                if (e <= f) jj += step;
+              }
+              const long long off = __shfl_sync(0xFFFFFFFFu, rowoff, jj) + f;
+              t[u] = -1;
+              w[u] = 0.0f;
+              if (f < total) {
+                t[u] = __ldg(v.idx + off);
+                w[u] = __ldg(v.w + off);
+              }
+            }
+#pragma unroll
+            for (int u = 0; u < 8; ++u)
+              if (t[u] >= 0) acc_add(base_a, base_b, (unsigned)(t[u] - (int)lo), wfix(w[u]));
+          }
         }
       }
     }
-    // ---- off the critical path, by each thread once its delivery share is done: the
-    // spike statistics of this CTA's spikes, and the next step's drive
-    for (int j = threadIdx.x; j < nspk; j += NT) {
-      const int n = s_spk[j];
+    // ---- tail, by warps as they finish delivering: the raster and the statistics of this
+    // rank's spikes (from the highest thread down, i.e. warps that had no delivery batch
+    // first), then the next step's drive in chunks of 32 neurons
+    for (int j = NT - 1 - threadIdx.x; j < nown; j += NT) {
+      const int n = s_own[j];
+      const long long pos = base + my_off + j;
+      if (pos < v.raster_cap) v.raster[pos] = n;
       SpikeStat st = v.sstat[n];
       st.nospks += 1;
       if (st.last >= 0) {
@@ -385,13 +616,24 @@ __device__ void team_run(const TeamItem &it, int rank, unsigned char *s_raw, int
       st.last = (int)t_abs;
       v.sstat[n] = st;
     }
-    if (prez && lt + 1 < it.steps)
-      for (int i = threadIdx.x; i < cnt; i += NT) s_z[i] = normal(v.seed, (uint64_t)(lo + i), (uint64_t)(t_abs + 1));
+    if (L.prez && lt + 1 < it.steps)
+      for (;;) {
+        int c = 0;
+        if (lane == 0) c = atomicAdd(&sh.work[par], 1);
+        c = __shfl_sync(0xFFFFFFFFu, c, 0) * 32;
+        if (c >= cnt) break;
+        const int i = c + lane;
+        if (i < cnt) s_z[i] = normal(v.seed, (uint64_t)(lo + i), (uint64_t)(t_abs + 1));
+      }
     __syncthreads();
+    if (gl && sh.fail) return;
     base += K;
   }
-  // pending currents (from the last delivery) back to global memory for the next launch
-  for (int i = threadIdx.x; i < cnt; i += NT) v.acc[lo + i] = (long long)s_a[i] * 65536 + s_b[i];
+  // pending currents (from the last delivery) and the state back to global memory
+  for (int i = threadIdx.x; i < cnt; i += NT) {
+    v.acc[lo + i] = (long long)s_a[i] * 65536 + s_b[i];
+    if (L.vu_sm) v.vu[lo + i] = s_vu[i];
+  }
   __syncthreads();
 }
 
@@ -401,19 +643,21 @@ __global__ void __launch_bounds__(NT, 1) k_team(const TeamItem *__restrict__ ite
                                                 const int *nslots, int *slot_head, unsigned long long limit_ns,
                                                 int stall) {
   extern __shared__ __align__(16) unsigned char s_raw[];
-  __shared__ int s_slot;
-  __shared__ int s_nspk;
-  __shared__ long long s_gpos;
+  __shared__ TeamShared sh;
   const int ns = *nslots;
   for (;;) {
-    if (threadIdx.x == 0) s_slot = atomicAdd(slot_head, 1);
+    if (threadIdx.x == 0) sh.slot = atomicAdd(slot_head, 1);
     __syncthreads();
-    const int sl = s_slot;
+    const int sl = sh.slot;
     __syncthreads();
     if (sl >= ns) break;
     const int2 x = slots[sl];
-    const TeamItem &it = items[x.x];
-    if (it.steps > 0) team_run<NT>(it, x.y, s_raw, &s_nspk, &s_gpos, limit_ns, stall);
+    // the network's descriptor in shared memory: read on every step's dependent chains
+    __shared__ TeamItem s_it;
+    if (threadIdx.x == 0) s_it = items[x.x];
+    __syncthreads();
+    if (s_it.steps > 0) team_run<NT>(s_it, x.y, s_raw, sh, limit_ns, stall);
+    __syncthreads();
   }
 }
 
@@ -422,7 +666,13 @@ __global__ void __launch_bounds__(NT, 1) k_team(const TeamItem *__restrict__ ite
 // ---------------------------------------------------------------------------------------
 constexpr int kTeamNT = 1024;
 
-size_t team_smem(int64_t rc) { return (size_t)rc * (rc <= kPrezSlice ? 16 : 12) + 16; }
+size_t team_smem(int64_t rc, int team) {
+  if (rc < 1 || team < 1 || team > kMaxTeam) return 0;
+  const int cap = team_window(rc, team);
+  if (team > 1 && cap == 0) return 0;
+  const size_t bytes = team_layout(rc, team, cap).bytes;
+  return bytes > kTeamSmemLimit ? 0 : (bytes < 16 ? 16 : bytes);
+}
 
 cudaError_t team_max_blocks(size_t smem, int *out) {
   cudaError_t e = cudaFuncSetAttribute(k_team<kTeamNT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

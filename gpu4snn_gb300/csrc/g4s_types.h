@@ -61,15 +61,18 @@ struct NetView {
 struct TeamItem {
   NetView v;
   const uint16_t *seg;  // [n][team+1] row segment offsets (team > 1)
-  int *list;            // [2][n] spike lists of the step, by step parity (team > 1)
+  unsigned long long *list;  // [4][n] tagged spike ids, by step parity: [par] beyond a rank's record
+                             // lines (at its neuron offset), [2 + par] the step's dense list
+  unsigned long long *rec;   // [2][team][2 x 16] tagged spike records, by step parity (zero at launch)
   int64_t t_abs0;       // absolute step of the first step of this launch
   int steps;            // steps of this launch (0: nothing to do)
   int last;             // this launch ends the run: record the input current at its last step
   int team;             // CTAs of the team
   int rc;               // neurons per CTA slice
-  GridSync *sync;       // team barrier and error word
+  GridSync *sync;       // error word of the team
   int mode;             // delivery mapping of a multi-CTA team (kDeliverRun or kDeliverLane)
-  int pad;
+  int cap;              // delivery window of a multi-CTA rank (spike ids in shared memory)
+  unsigned tag0;        // record tag of step lt: tag0 + lt + 1 (never repeats for the list's words)
 };
 
 // Delivery mappings of a multi-CTA team: warps walk the concatenated segments of 32
