@@ -47,6 +47,8 @@ constexpr int64_t kBatchSlice = 2048;          // neurons per CTA of a batched n
 constexpr int kMaxTeam = 192;                  // CTAs of one team (three record slots per thread)
 constexpr int kMinWindow = 1024;               // spike ids a multi-CTA rank can stage per delivery window
 constexpr int kMaxWindow = 4096;
+constexpr int kFlatMax = 8192;                 // synapses of a step a rank delivers flat (else by runs)
+constexpr int64_t kFlatSlice = 4096;           // ... on slices up to this size
 // Spike records of a multi-CTA team: per rank and step parity kRecLines lines of 16
 // tagged 64-bit words (count, then up to 16 kRecLines - 1 ids); readers fetch the second
 // line of a rank only if it had more than 15 spikes in the previous step.
@@ -56,8 +58,8 @@ constexpr int kRecWords = 16;
 // Shared-memory layout of one team rank (byte offsets; the optional arrays are present
 // when their flag is set).  `cap` is the delivery window of a multi-CTA team (0 for one CTA).
 struct TeamLayout {
-  unsigned abcd, vu, a, b, own, z, cnt, off, xoff, inl, pay, spk, bytes;
-  bool abcd_sm, vu_sm, prez;
+  unsigned abcd, vu, a, b, own, z, cnt, off, xoff, inl, pay, spk, sb, pre, ex, wsum, bytes;
+  bool abcd_sm, vu_sm, prez, flat;
 };
 __host__ __device__ inline unsigned team_align16(size_t x) { return (unsigned)((x + 15) & ~(size_t)15); }
 __host__ __device__ inline TeamLayout team_layout(int64_t rc, int team, int cap) {
@@ -65,6 +67,7 @@ __host__ __device__ inline TeamLayout team_layout(int64_t rc, int team, int cap)
   L.abcd_sm = rc <= kAbcdSlice;
   L.vu_sm = rc <= kVuSlice;
   L.prez = rc <= kPrezSlice;
+  L.flat = team > 1 && rc <= kFlatSlice;
   size_t o = 0;
   L.abcd = (unsigned)o;
   if (L.abcd_sm) o += (size_t)rc * 16;
@@ -78,7 +81,7 @@ __host__ __device__ inline TeamLayout team_layout(int64_t rc, int team, int cap)
   o = team_align16(o + (size_t)rc * 4);
   L.z = (unsigned)o;
   if (L.prez) o = team_align16(o + (size_t)rc * 4);
-  L.cnt = L.off = L.xoff = L.inl = L.pay = L.spk = (unsigned)o;
+  L.cnt = L.off = L.xoff = L.inl = L.pay = L.spk = L.sb = L.pre = L.ex = L.wsum = (unsigned)o;
   if (team > 1) {
     L.cnt = (unsigned)o;  // spikes per rank
     o = team_align16(o + (size_t)(team + 1) * 4);
@@ -92,6 +95,17 @@ __host__ __device__ inline TeamLayout team_layout(int64_t rc, int team, int cap)
     o = team_align16(o + (size_t)team * kRecLines * kRecWords * 4);
     L.spk = (unsigned)o;  // the delivery window: spike ids of the step
     o = team_align16(o + (size_t)cap * 4);
+    L.sb = L.pre = L.ex = L.wsum = (unsigned)o;
+  }
+  if (L.flat) {
+    L.sb = (unsigned)o;  // flat delivery: first slot of each spike's segment
+    o = team_align16(o + (size_t)cap * 2);
+    L.pre = (unsigned)o;  // ... offset of each spike's segment in the concatenation
+    o = team_align16(o + (size_t)(cap + 1) * 4);
+    L.ex = (unsigned)o;  // ... spike of every synapse of the concatenation
+    o = team_align16(o + (size_t)kFlatMax * 2);
+    L.wsum = (unsigned)o;  // ... per-warp sums of the scan
+    o = team_align16(o + 33 * 4);
   }
   L.bytes = (unsigned)o;
   return L;
@@ -100,10 +114,11 @@ __host__ __device__ inline TeamLayout team_layout(int64_t rc, int team, int cap)
 // kMaxWindow ids; 0 if less than kMinWindow is left (the geometry does not fit).
 inline int team_window(int64_t rc, int team) {
   if (team <= 1) return 0;
-  const size_t base = team_layout(rc, team, 0).bytes;
-  if (base + (size_t)kMinWindow * 4 > kTeamSmemLimit) return 0;
-  const size_t cap = (kTeamSmemLimit - base) / 4;
-  return (int)(cap > (size_t)kMaxWindow ? kMaxWindow : cap & ~(size_t)3);
+  const size_t kPerId = rc <= kFlatSlice ? 4 + 2 + 4 : 4;  // id (segment start, segment offset)
+  const size_t base = team_layout(rc, team, 0).bytes + 64;  // + alignment of the arrays
+  if (base + (size_t)kMinWindow * kPerId > kTeamSmemLimit) return 0;
+  const size_t cap = (kTeamSmemLimit - base) / kPerId;
+  return (int)(cap > (size_t)kMaxWindow ? kMaxWindow : cap & ~(size_t)7);
 }
 cudaError_t launch_sort_rows(const NetView &v, cudaStream_t s);
 cudaError_t launch_segoff(const NetView &v, int team, int64_t rc, uint16_t *seg, cudaStream_t s);

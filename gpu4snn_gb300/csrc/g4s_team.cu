@@ -182,7 +182,9 @@ struct TeamShared {
 constexpr int kRankWords = kRecLines * kRecWords;
 constexpr int kInline = kRankWords - 1;
 constexpr int kSlots = (kMaxTeam * kRankWords / 2 + 1023) / 1024;
-constexpr int kLine1After = 7;  // line 1 of a rank is read if it had more spikes in the previous step
+constexpr int kLine1After = 7;
+constexpr unsigned long long kPrefetchBudget = 64ull << 20;  // table bytes per step prefetched into L2
+constexpr int kFlatMinSpikes = 128;  // fewer spikes: run delivery (the flat one's scan costs more)  // line 1 of a rank is read if it had more spikes in the previous step
 
 // Gives up a wait: first error wins, every CTA of the team leaves at its next check.
 __device__ __forceinline__ void give_up(TeamShared &sh, GridSync *gs) {
@@ -226,6 +228,10 @@ __device__ void team_run(const TeamItem &it, int rank, unsigned char *s_raw, Tea
   int *s_xoff = reinterpret_cast<int *>(s_raw + L.xoff);
   int *s_inl = reinterpret_cast<int *>(s_raw + L.inl);
   unsigned *s_pay = reinterpret_cast<unsigned *>(s_raw + L.pay);
+  uint16_t *s_sb = reinterpret_cast<uint16_t *>(s_raw + L.sb);
+  int *s_pre = reinterpret_cast<int *>(s_raw + L.pre);
+  uint16_t *s_ex = reinterpret_cast<uint16_t *>(s_raw + L.ex);
+  int *s_wsum = reinterpret_cast<int *>(s_raw + L.wsum);
   int *s_spk = reinterpret_cast<int *>(s_raw + L.spk);
   const int64_t lo = min((int64_t)rank * rc, v.n);
   const int64_t hi = min(lo + rc, v.n);
@@ -237,6 +243,21 @@ __device__ void team_run(const TeamItem &it, int rank, unsigned char *s_raw, Tea
   constexpr int kWarps = NT / 32;
   const bool solo = T == 1;   // the whole network in this CTA: no exchange
   const bool lead = rank == 0 && threadIdx.x == 0;
+  // A spiking neuron's owner asks L2 for its table row (and segment offsets) as soon as the
+  // spike is known, so the whole team's reads of the row, a few microseconds later, hit
+  // L2; skipped while the previous step's rows exceeded kPrefetchBudget, or if the tables
+  // are not 16-byte aligned (caller-owned arrays).
+  const unsigned row_bytes = (unsigned)v.stride * 4u;
+  const bool pf_ok = ((reinterpret_cast<uintptr_t>(v.idx) | reinterpret_cast<uintptr_t>(v.w)) & 15) == 0;
+  auto prefetch_row = [&](int64_t n) {
+    prefetch_l2_bulk(v.idx + (size_t)n * v.stride, row_bytes);
+    prefetch_l2_bulk(v.w + (size_t)n * v.stride, row_bytes);
+    if (!solo) {
+      const char *so = reinterpret_cast<const char *>(it.seg + (size_t)n * segw);
+      for (unsigned b = 0; b < segw * 2u; b += 128) prefetch_l2_line(so + b);
+      prefetch_l2_line(so + segw * 2u - 1u);
+    }
+  };
   // neuron state of the slice: shared memory for the launch when it fits, else global
   float2 *vu = L.vu_sm ? s_vu : v.vu + lo;
   const float4 *abcd = L.abcd_sm ? s_abcd : v.abcd + lo;
@@ -258,6 +279,7 @@ __device__ void team_run(const TeamItem &it, int rank, unsigned char *s_raw, Tea
   __syncthreads();
 
   long long base = 0;
+  int k_prev = 0;  // spikes of the team in the previous step
   for (int lt = 0; lt < it.steps; ++lt) {
     const int64_t t_abs = it.t_abs0 + lt;
     const bool last = it.last && lt == it.steps - 1;
@@ -270,6 +292,7 @@ __device__ void team_run(const TeamItem &it, int rank, unsigned char *s_raw, Tea
       v.base[lt] = base;
       if (v.stamps) v.stamps[2 * lt] = globaltimer();
     }
+    const bool pf = pf_ok && (unsigned long long)k_prev * row_bytes * 2ull <= kPrefetchBudget;
     // ---- update of the owned neurons, two per thread per round with the loads first
     for (int i0 = threadIdx.x; i0 < cnt; i0 += 2 * NT) {
       const int i1 = i0 + NT;
@@ -298,6 +321,10 @@ __device__ void team_run(const TeamItem &it, int rank, unsigned char *s_raw, Tea
         v.ilast[n0] = I0;
         if (h1) v.ilast[n1] = I1;
       }
+      if (pf) {
+        if (k0) prefetch_row(n0);
+        if (k1) prefetch_row(n1);
+      }
       if (k0) s_own[atomicAdd(&sh.nown[par], 1)] = (int)n0;
       if (k1) s_own[atomicAdd(&sh.nown[par], 1)] = (int)n1;
     }
@@ -321,7 +348,11 @@ __device__ void team_run(const TeamItem &it, int rank, unsigned char *s_raw, Tea
     const unsigned long long *recs = it.rec + (size_t)par * T * kRankWords;
     const unsigned long long *ovf_all = it.list + (size_t)par * v.n;
     unsigned long long *dense = it.list + (size_t)(2 + par) * v.n;
-    bool gl = false;  // the step's ids are read from the dense list in global memory
+    bool gl = false;    // the step's ids are read from the dense list in global memory
+    bool flat = false;  // flat delivery from shared memory
+    int F = 0;          // ... synapses of the concatenated segments
+    const bool zwant = L.prez && lt + 1 < it.steps;  // the next step's drive is precomputed
+    int zdone = 0;      // ... for neurons [0, zdone) already
     if (!solo) {
       // ---- publish: both record lines of this rank (count, ids, padding), ids beyond
       // them in the overflow list; every word tagged with the step, so no fence is needed
@@ -462,6 +493,57 @@ __device__ void team_run(const TeamItem &it, int rank, unsigned char *s_raw, Tea
         __syncthreads();
         if (sh.fail) return;
       }
+      if (!solo && !gl && K >= kFlatMinSpikes && L.flat) {
+        // segment bounds and their offsets in the concatenation (for the flat delivery):
+        // thread t takes spikes 4t .. 4t+3 (K <= cap <= 4 NT); a block scan of their
+        // lengths (every warp scans the warp sums itself), then each thread marks the
+        // synapses of its spikes with the spike's index
+        const uint64_t pkeep = policy_evict_last();
+        int len[4], b4[4], sum = 0;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int q = threadIdx.x * 4 + u;
+          len[u] = 0;
+          b4[u] = 0;
+          if (q < K) {
+            const uint16_t *so = it.seg + (size_t)s_spk[q] * segw + rank;
+            b4[u] = ld_keep_u16(so, pkeep);
+            len[u] = ld_keep_u16(so + 1, pkeep) - b4[u];
+          }
+          sum += len[u];
+        }
+        int incl = sum;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+          if (lane >= o) incl += y;
+        }
+        if (lane == 31) s_wsum[warp] = incl;
+        __syncthreads();
+        const int ws = s_wsum[lane];
+        int wi = ws;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int y = __shfl_up_sync(0xFFFFFFFFu, wi, o);
+          if (lane >= o) wi += y;
+        }
+        F = __shfl_sync(0xFFFFFFFFu, wi, 31);
+        flat = F <= kFlatMax;
+        if (flat) {
+          int pre = __shfl_sync(0xFFFFFFFFu, wi - ws, warp) + incl - sum;
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            const int q = threadIdx.x * 4 + u;
+            if (q < K) {
+              s_pre[q] = pre;
+              s_sb[q] = (uint16_t)b4[u];
+              for (int f = pre; f < pre + len[u]; ++f) s_ex[f] = (uint16_t)q;
+            }
+            pre += len[u];
+          }
+        }
+        __syncthreads();
+      }
       if (solo) {
         // ---- delivery, one-CTA team: flat over K whole rows of stride/4 vectors
         const int rv = v.stride >> 2;
@@ -491,6 +573,33 @@ __device__ void team_run(const TeamItem &it, int rank, unsigned char *s_raw, Tea
             q += 1;
           }
         }
+      } else if (flat) {
+        // ---- delivery, larger team, flat: each thread walks synapses f = tid, tid + NT,
+        // ... of the concatenated segments (consecutive lanes, consecutive synapses),
+        // eight table reads in flight, no shuffles; its next-step drive is computed
+        // while the reads are in flight
+        for (int f0 = threadIdx.x, pass = 0; pass == 0 || f0 < F; f0 += 8 * NT, ++pass) {
+          int t[8];
+          float w[8];
+#pragma unroll
+          for (int u = 0; u < 8; ++u) {
+            const int f = f0 + u * NT;
+            t[u] = -1;
+            w[u] = 0.0f;
+            if (f < F) {
+              const int q = s_ex[f];
+              const long long off = (long long)s_spk[q] * v.stride + s_sb[q] + (f - s_pre[q]);
+              t[u] = __ldg(v.idx + off);
+              w[u] = __ldg(v.w + off);
+            }
+          }
+          if (pass == 0 && zwant && threadIdx.x < cnt)
+            s_z[threadIdx.x] = normal(v.seed, (uint64_t)(lo + threadIdx.x), (uint64_t)(t_abs + 1));
+#pragma unroll
+          for (int u = 0; u < 8; ++u)
+            if (t[u] >= 0) acc_add(base_a, base_b, (unsigned)(t[u] - (int)lo), wfix(w[u]));
+        }
+        zdone = zwant ? min(cnt, NT) : 0;
       } else if (it.mode == kDeliverLane) {
         // ---- delivery, larger team, one lane per spike: each lane walks its own segment,
         // four synapses (eight loads) at a time; the warp's next 32 spike ids and segment
@@ -616,11 +725,11 @@ __device__ void team_run(const TeamItem &it, int rank, unsigned char *s_raw, Tea
       st.last = (int)t_abs;
       v.sstat[n] = st;
     }
-    if (L.prez && lt + 1 < it.steps)
+    if (zwant)
       for (;;) {
         int c = 0;
         if (lane == 0) c = atomicAdd(&sh.work[par], 1);
-        c = __shfl_sync(0xFFFFFFFFu, c, 0) * 32;
+        c = __shfl_sync(0xFFFFFFFFu, c, 0) * 32 + zdone;
         if (c >= cnt) break;
         const int i = c + lane;
         if (i < cnt) s_z[i] = normal(v.seed, (uint64_t)(lo + i), (uint64_t)(t_abs + 1));
@@ -628,6 +737,7 @@ __device__ void team_run(const TeamItem &it, int rank, unsigned char *s_raw, Tea
     __syncthreads();
     if (gl && sh.fail) return;
     base += K;
+    k_prev = K;
   }
   // pending currents (from the last delivery) and the state back to global memory
   for (int i = threadIdx.x; i < cnt; i += NT) {
