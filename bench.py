@@ -45,9 +45,13 @@ WORKLOADS = {
     "n25k": (25_000, 1000, 500, 1.0, 5),  # small profiling case: 0.2 GB of tables, still > L2
     "n300k": (300_000, 1000, 50, 1.0, 6),  # profiling case for large-N delivery: 2.4 GB of tables
 }
-# algorithmic bytes: delivery = spikes x Nsyn x (4 B target + 4 B weight); update per
-# neuron and step = v,u read+write (16) + a,b,c,d (16) + current read (8)
+# algorithmic bytes: delivery = spikes x Nsyn x (4 B target + 4 B weight) and the spike
+# statistics (32 B read + 32 B written per spike); the neuron state (v,u read+write 16 B,
+# a,b,c,d 16 B, current 8 B per neuron and step) only when it is not kept on chip: the team
+# kernel holds slices of up to RESIDENT_SLICE neurons in shared memory for a whole launch
 UPDATE_BYTES_PER_NEURON = 40
+STAT_BYTES_PER_SPIKE = 64
+RESIDENT_SLICE = 2048
 
 
 def peaks():
@@ -305,11 +309,18 @@ def served_leg(g, count, lams):
     return out
 
 
-def load_traffic(name):
-    p = os.path.join(ROOT, "profiles", "persistent_step_traffic.json")
-    if os.path.exists(p):
-        d = json.load(open(p))
-        return d.get(name)
+def load_traffic(name, steps_per_launch):
+    """DRAM bytes (read + written) per launch of the team kernel on this workload, from the
+    committed ncu summary (a table row `| workload | steps per launch | bytes per launch |`),
+    scaled to this launch's steps; None if the workload was not captured."""
+    import re
+    p = os.path.join(ROOT, "profiles", "k_team_dram_traffic.md")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        m = re.match(r"^\|\s*(\w+)\s*\|\s*(\d+)\s*\|\s*([0-9.eE+]+)\s*\|", line)
+        if m and m.group(1) == name:
+            return float(m.group(3)) * steps_per_launch / int(m.group(2))
     return None
 
 
@@ -378,14 +389,15 @@ def main():
     ev_all = reduce_sum(pg, float(events))
     value = ev_all / (t_max * 1e-3)
     peak, peak_kind = peaks()
+    team, slice_ = net.geometry()
+    last_alg = int(runs[-1][6])
+    resident = last_alg == g.ALG_SKL and team > 0 and slice_ <= RESIDENT_SLICE
     deliv_bytes = events * 8
-    upd_bytes = n * T * a.steps * UPDATE_BYTES_PER_NEURON
+    upd_bytes = spikes * STAT_BYTES_PER_SPIKE + (0 if resident else n * T * a.steps * UPDATE_BYTES_PER_NEURON)
     n_launch = max(1, launches)
     achieved = (deliv_bytes + upd_bytes) / n_launch / (kern_ms / n_launch * 1e-3) / 1e9
     upd_ms = sum(r[4] for r in runs)
     deliv_ms = max(1e-9, sum(r[5] for r in runs) - upd_ms)
-    team, slice_ = net.geometry()
-    last_alg = int(runs[-1][6])
     if last_alg == g.ALG_SKL and team > 0:
         kname = f"k_team (SKL team kernel: {team} CTAs x 1024 threads, {slice_} neurons per CTA)"
     elif last_alg == g.ALG_SKL:
@@ -394,7 +406,9 @@ def main():
         kname = f"k_update + k_deliver ({ALG_LABEL[last_alg]})"
     roofline = {"kernel": kname, "bound": "hbm",
                 "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "peak_source": f"{peak_kind} hbm_gbs", "traffic": load_traffic(a.workload),
+                "peak_source": f"{peak_kind} hbm_gbs",
+                "traffic": load_traffic(a.workload, T) if last_alg == g.ALG_SKL and team > 0 else None,
+                "state_on_chip": resident,
                 "algorithmic_bytes_per_launch": (deliv_bytes + upd_bytes) / n_launch,
                 "launch_ms": kern_ms / n_launch,
                 "delivery_phase": {"bytes": deliv_bytes, "ms": deliv_ms, "gbs": deliv_bytes / deliv_ms / 1e6,

@@ -41,7 +41,9 @@ constexpr int64_t kVuSlice = 2048;             // ... keep v, u in shared memory
 constexpr int64_t kAbcdSlice = 2048;           // ... keep a, b, c, d in shared memory (larger slices
                                                // keep them in global memory: the L1 left by a larger
                                                // shared-memory carve-out holds fewer table loads in flight)
-constexpr int64_t kSoloSlice = 2048;           // neurons per CTA of a network running alone
+constexpr int64_t kSoloSlice = 128;            // neurons per CTA of a network running alone (at
+                                               // most: it spreads over every SM; measured best from
+                                               // N = 2500 to 10^6)
 constexpr int64_t kBatchSlice = 2048;          // neurons per CTA of a batched network (measured: fewer,
                                                // larger slices made the config-4 ensemble 1.4x slower)
 constexpr int kMaxTeam = 192;                  // CTAs of one team (three record slots per thread)
