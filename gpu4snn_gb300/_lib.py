@@ -127,6 +127,10 @@ SIGNATURES = [
     ("g4s_server_release", C.c_int, [_P, C.c_int64]),
     ("g4s_server_get_stats", C.c_int, [_P, C.POINTER(ServerStats)]),
     ("g4s_server_stop", C.c_int, [_P, C.c_int32]),
+    ("g4s_net_stream_raster", C.c_int, [_P, C.c_char_p]),
+    ("g4s_net_write_raster_file", C.c_int, [_P, C.c_char_p]),
+    ("g4s_net_save_tables", C.c_int, [_P, C.c_char_p]),
+    ("g4s_net_create_from_file", C.c_int, [C.POINTER(NetDesc), C.c_char_p, C.POINTER(_P)]),
     ("g4s_pinned_alloc", C.c_int, [C.c_uint64, C.POINTER(_P)]),
     ("g4s_pinned_free", C.c_int, [_P]),
 ]

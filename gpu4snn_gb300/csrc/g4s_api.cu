@@ -154,6 +154,8 @@ struct g4s_net {
   // autotuner: this handle's measured choice
   bool tuned = false;
   TuneChoice tune;
+  // raster streamed to a binary file (while set, the raster is not kept in host memory)
+  RasterFile *rstream = nullptr;
 };
 
 static std::atomic<int> g_fail_next_alloc{0};
@@ -161,6 +163,10 @@ static std::atomic<int> g_fail_next_alloc{0};
 static void free_net(g4s_net *n) {
   if (!n) return;
   NetView &v = n->v;
+  if (n->rstream) {
+    raster_close(n->rstream);
+    n->rstream = nullptr;
+  }
   cudaFree(v.vu);
   cudaFree(v.abcd);
   cudaFree(v.acc);
@@ -317,6 +323,12 @@ static int check_status(g4s_net *n, const char *what) {
 
 static int reset_net(g4s_net *n) {
   NetView &v = n->v;
+  if (n->rstream) {  // the step numbering restarts: a streamed raster ends here
+    RasterFile *f = n->rstream;
+    n->rstream = nullptr;
+    int rc = raster_close(f);
+    if (rc) return rc;
+  }
   set_drive(n);
   G4S_CUDA(cudaMemsetAsync(v.status, 0, sizeof(int), n->stream));
   G4S_CUDA(cudaMemsetAsync(n->gs, 0, sizeof(GridSync), n->stream));
@@ -554,7 +566,10 @@ static int chunk_copy_raster(g4s_net *n, int cs, cudaStream_t s) {
 
 static void chunk_finish(g4s_net *n, int cs, int64_t *spikes) {
   const int64_t total = chunk_total(n, cs);
-  if (n->desc.record_raster && total > 0) {
+  if (n->desc.record_raster && n->rstream) {
+    for (int lt = 0; lt < cs; ++lt) std::sort(n->h_raster + n->h_base[lt], n->h_raster + n->h_base[lt] + n->h_counts[lt]);
+    raster_push(n->rstream, n->h_counts, cs, n->h_raster, total);
+  } else if (n->desc.record_raster && total > 0) {
     const size_t off = n->rt.size();
     n->rt.resize(off + (size_t)total);
     n->rid.resize(off + (size_t)total);
@@ -1319,6 +1334,74 @@ int g4s_run_protocol(int32_t n, int32_t nsyn, int32_t iterations, int32_t algori
 int g4s_conn_glibc(uint32_t seed, int32_t n, int32_t nsyn, int32_t stride, int32_t *idx, float *w) {
   if (!idx || !w) return set_error(G4S_ERR_INVALID, "null table buffer");
   return conn_glibc_host(seed, n, nsyn, stride, idx, w);
+}
+
+int g4s_net_stream_raster(g4s_net *n, const char *path) {
+  if (!n) return set_error(G4S_ERR_INVALID, "null handle");
+  if (n->rstream) {
+    RasterFile *f = n->rstream;
+    n->rstream = nullptr;
+    int rc = raster_close(f);
+    if (rc) return rc;
+  }
+  if (!path) return G4S_OK;
+  if (!n->desc.record_raster) return set_error(G4S_ERR_STATE, "the raster is not recorded (record_raster = 0)");
+  return raster_open(path, n->v.n, n->t_abs, &n->rstream);
+}
+
+int g4s_net_write_raster_file(g4s_net *n, const char *path) {
+  if (!n || !path) return set_error(G4S_ERR_INVALID, "null argument");
+  if (n->rid.size() != (size_t)n->total_spikes || n->counts.size() != (size_t)n->t_abs)
+    return set_error(G4S_ERR_STATE, "the host raster does not hold every step since the reset "
+                                    "(not recorded, or streamed to a file)");
+  return raster_write_all(path, n->v.n, 0, n->counts, n->rid);
+}
+
+int g4s_net_save_tables(g4s_net *n, const char *path) {
+  if (!n || !path) return set_error(G4S_ERR_INVALID, "null argument");
+  const size_t cnt = (size_t)n->v.n * (size_t)n->v.stride;
+  std::vector<int32_t> idx;
+  std::vector<float> w;
+  try {
+    idx.resize(cnt);
+    w.resize(cnt);
+  } catch (...) {
+    return set_error(G4S_ERR_NOMEM, "host tables");
+  }
+  int rc = g4s_net_tables(n, 0, n->v.n, idx.data(), w.data());
+  if (rc) return rc;
+  TableHeader h{};
+  h.n = n->v.n;
+  h.nsyn = n->v.nsyn;
+  h.stride = n->v.stride;
+  h.seed = n->desc.seed;
+  h.conn_law = n->desc.conn_law;
+  h.self_loops = n->desc.self_loops;
+  h.exc_permille = n->desc.exc_permille;
+  h.flags = 1;
+  return tables_write(path, h, idx.data(), w.data());
+}
+
+int g4s_net_create_from_file(const g4s_net_desc *desc, const char *path, g4s_net **out) {
+  if (!desc || !path || !out) return set_error(G4S_ERR_INVALID, "null argument");
+  *out = nullptr;
+  TableHeader h{};
+  int rc = tables_read_header(path, &h);
+  if (rc) return rc;
+  if (h.n != desc->n || h.nsyn != desc->nsyn)
+    return set_error(G4S_ERR_INVALID, std::string(path) + " holds a network of n=" + std::to_string(h.n) +
+                                          ", nsyn=" + std::to_string(h.nsyn));
+  const size_t cnt = (size_t)h.n * (size_t)h.stride;
+  std::vector<int32_t> idx;
+  std::vector<float> w;
+  try {
+    idx.resize(cnt);
+    w.resize(cnt);
+  } catch (...) {
+    return set_error(G4S_ERR_NOMEM, "host tables");
+  }
+  if ((rc = tables_read(path, h, idx.data(), w.data()))) return rc;
+  return g4s_net_create_from_tables(desc, idx.data(), w.data(), h.stride, out);
 }
 
 }  // extern "C"

@@ -4,6 +4,7 @@
 
 #include <cstdint>
 #include <string>
+#include <vector>
 
 #include "g4s_types.h"
 
@@ -131,6 +132,24 @@ cudaError_t launch_team(const TeamItem *items, const int2 *slots, const int *nsl
 cudaError_t team_max_blocks(size_t smem, int *out);
 // shared memory of one rank of a team of `team` CTAs with `rc` neurons each (0: does not fit)
 size_t team_smem(int64_t rc, int team);
+
+// Binary files (g4s_formats.cu): the raster, streamed by a writer thread, and the tables.
+struct RasterFile;
+int raster_open(const char *path, int64_t n, int64_t t0, RasterFile **out);
+void raster_push(RasterFile *f, const int32_t *counts, int cs, const int32_t *ids, int64_t nids);
+int raster_close(RasterFile *f);
+int raster_write_all(const char *path, int64_t n, int64_t t0, const std::vector<int32_t> &counts,
+                     const std::vector<int32_t> &ids);
+struct TableHeader {
+  int64_t n;
+  int32_t nsyn, stride;
+  uint64_t seed;
+  int32_t conn_law, self_loops, exc_permille, flags;  // flags: 1 = rows sorted by target
+  int32_t pad[2];
+};
+int tables_write(const char *path, const TableHeader &h, const int32_t *idx, const float *w);
+int tables_read_header(const char *path, TableHeader *h);
+int tables_read(const char *path, const TableHeader &h, int32_t *idx, float *w);
 
 // Error reporting (thread-local message behind g4s_last_error()).
 int set_error(int code, const std::string &msg);

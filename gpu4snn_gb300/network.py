@@ -35,17 +35,21 @@ class Network:
     self_loops    allow a neuron to target itself (the reference's generator does)
     conn_law      CONN_PHILOX (GPU generator) or CONN_GLIBC (the reference's rand() law)
     tables        optional (idx, w) host arrays [n][stride] to upload instead
+    tables_file   optional tables checkpoint (save_tables) to build from instead
     """
 
     def __init__(self, n: int, nsyn: int, seed: int = 1, drive_scale: float = 1.0, self_loops: bool = False,
                  conn_law: int = CONN_PHILOX, exc_permille: int = 800, record_raster: bool = True,
-                 raster_budget_bytes: int = 0, tables: tuple[np.ndarray, np.ndarray] | None = None):
+                 raster_budget_bytes: int = 0, tables: tuple[np.ndarray, np.ndarray] | None = None,
+                 tables_file: str | None = None):
         L = load()
         self.desc = _lib.NetDesc(n=n, nsyn=nsyn, exc_permille=exc_permille, self_loops=int(self_loops),
                                  conn_law=conn_law, seed=seed, drive_scale=drive_scale,
                                  record_raster=int(record_raster), raster_budget_bytes=raster_budget_bytes)
         h = C.c_void_p()
-        if tables is None:
+        if tables_file is not None:
+            check(L.g4s_net_create_from_file(C.byref(self.desc), tables_file.encode(), C.byref(h)))
+        elif tables is None:
             check(L.g4s_net_create(C.byref(self.desc), C.byref(h)))
         else:
             idx = np.ascontiguousarray(tables[0], dtype=np.int32)
@@ -161,6 +165,18 @@ class Network:
 
     def write_results(self, directory: str, elapsed_ms: float, elapsed_with_data_ms: float):
         check(load().g4s_net_write_results(self._h, directory.encode(), None, elapsed_ms, elapsed_with_data_ms))
+
+    def stream_raster(self, path: str | None):
+        """Stream the raster of the following runs to a binary file (None ends the stream);
+        read it with gpu4snn_gb300.formats.read_raster."""
+        check(load().g4s_net_stream_raster(self._h, None if path is None else path.encode()))
+
+    def write_raster_file(self, path: str):
+        check(load().g4s_net_write_raster_file(self._h, path.encode()))
+
+    def save_tables(self, path: str):
+        """Checkpoint the (sorted) tables; Network(..., tables_file=path) rebuilds from it."""
+        check(load().g4s_net_save_tables(self._h, path.encode()))
 
 
 def run_batch(nets: list[Network], steps) -> tuple[float, int]:

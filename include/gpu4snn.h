@@ -162,6 +162,26 @@ int g4s_inject_fault(g4s_net *net, int32_t kind);
 int g4s_net_write_results(g4s_net *net, const char *dir, const float *init_state /* [9][n] or NULL */,
                           double elapsed_ms, double elapsed_with_data_ms);
 
+/* Binary files (the reference writes its raster as text rows from a per-step host scan,
+ * gpu4snn.cu:1256-1261, and regenerates its tables for every run, gpu4snn.cu:862-911).
+ * Raster file "G4SRAS01" (little-endian): char[8] magic; int64 n; int64 first step;
+ * int64 steps; int64 spikes; then chunks to the end of the file: int32 cs; int32
+ * counts[cs]; int32 ids[sum counts], ascending within each step.
+ * g4s_net_stream_raster(net, path) writes the raster of the following runs to `path`, one
+ * chunk per device chunk, from a writer thread while the GPU computes the next chunk; the
+ * raster is then not kept in host memory.  path = NULL (or a reset, or destroy) ends the
+ * stream and completes the header.  Needs record_raster; G4S_ERR_IO if a write fails.
+ * g4s_net_write_raster_file writes the host raster of every step since the reset. */
+int g4s_net_stream_raster(g4s_net *net, const char *path);
+int g4s_net_write_raster_file(g4s_net *net, const char *path);
+/* Tables checkpoint "G4STAB01": char[8] magic; int64 n; int32 nsyn; int32 stride; uint64
+ * seed; int32 conn_law; int32 self_loops; int32 exc_permille; int32 flags (1 = rows sorted
+ * by target); int32 reserved[2]; int32 idx[n][stride]; float w[n][stride].
+ * g4s_net_create_from_file builds a network from such a file (desc->n and desc->nsyn must
+ * match it; desc->seed still seeds the neuron parameters and the drive). */
+int g4s_net_save_tables(g4s_net *net, const char *path);
+int g4s_net_create_from_file(const g4s_net_desc *desc, const char *path, g4s_net **out);
+
 /* The reference's whole experiment (main, gpu4snn.cu:735-1332): for each drive mode
  * (0..2, or `mode`) and scheme (0..4, or `algorithm`), run `iterations` steps of the same
  * network and write Results/N{n}Nsyn{nsyn}Regime{mode}Alg{alg}/ under results_root. */
