@@ -190,14 +190,6 @@ __device__ __forceinline__ float4 ld_stream_f4(const float4 *p, uint64_t pol) {
                : "l"(p), "l"(pol));
   return r;
 }
-// L2 prefetches: a whole table row by one bulk (TMA) request (16-byte aligned address, size
-// a multiple of 16), or one 128-byte line.
-__device__ __forceinline__ void prefetch_l2_bulk(const void *p, unsigned bytes) {
-  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ void prefetch_l2_line(const void *p) {
-  asm volatile("prefetch.global.L2::evict_last [%0];" ::"l"(p));
-}
 // The per-row segment table is small and read for every spike: keep it in L2.
 __device__ __forceinline__ uint64_t policy_evict_last() {
   uint64_t pol;

@@ -183,7 +183,6 @@ constexpr int kRankWords = kRecLines * kRecWords;
 constexpr int kInline = kRankWords - 1;
 constexpr int kSlots = (kMaxTeam * kRankWords / 2 + 1023) / 1024;
 constexpr int kLine1After = 7;
-constexpr unsigned long long kPrefetchBudget = 64ull << 20;  // table bytes per step prefetched into L2
 constexpr int kFlatMinSpikes = 128;  // fewer spikes: run delivery (the flat one's scan costs more)  // line 1 of a rank is read if it had more spikes in the previous step
 
 // Gives up a wait: first error wins, every CTA of the team leaves at its next check.
@@ -243,21 +242,6 @@ __device__ void team_run(const TeamItem &it, int rank, unsigned char *s_raw, Tea
   constexpr int kWarps = NT / 32;
   const bool solo = T == 1;   // the whole network in this CTA: no exchange
   const bool lead = rank == 0 && threadIdx.x == 0;
-  // A spiking neuron's owner asks L2 for its table row (and segment offsets) as soon as the
-  // spike is known, so the whole team's reads of the row, a few microseconds later, hit
-  // L2; skipped while the previous step's rows exceeded kPrefetchBudget, or if the tables
-  // are not 16-byte aligned (caller-owned arrays).
-  const unsigned row_bytes = (unsigned)v.stride * 4u;
-  const bool pf_ok = ((reinterpret_cast<uintptr_t>(v.idx) | reinterpret_cast<uintptr_t>(v.w)) & 15) == 0;
-  auto prefetch_row = [&](int64_t n) {
-    prefetch_l2_bulk(v.idx + (size_t)n * v.stride, row_bytes);
-    prefetch_l2_bulk(v.w + (size_t)n * v.stride, row_bytes);
-    if (!solo) {
-      const char *so = reinterpret_cast<const char *>(it.seg + (size_t)n * segw);
-      for (unsigned b = 0; b < segw * 2u; b += 128) prefetch_l2_line(so + b);
-      prefetch_l2_line(so + segw * 2u - 1u);
-    }
-  };
   // neuron state of the slice: shared memory for the launch when it fits, else global
   float2 *vu = L.vu_sm ? s_vu : v.vu + lo;
   const float4 *abcd = L.abcd_sm ? s_abcd : v.abcd + lo;
@@ -279,7 +263,6 @@ __device__ void team_run(const TeamItem &it, int rank, unsigned char *s_raw, Tea
   __syncthreads();
 
   long long base = 0;
-  int k_prev = 0;  // spikes of the team in the previous step
   for (int lt = 0; lt < it.steps; ++lt) {
     const int64_t t_abs = it.t_abs0 + lt;
     const bool last = it.last && lt == it.steps - 1;
@@ -292,7 +275,6 @@ __device__ void team_run(const TeamItem &it, int rank, unsigned char *s_raw, Tea
       v.base[lt] = base;
       if (v.stamps) v.stamps[2 * lt] = globaltimer();
     }
-    const bool pf = pf_ok && (unsigned long long)k_prev * row_bytes * 2ull <= kPrefetchBudget;
     // ---- update of the owned neurons, two per thread per round with the loads first
     for (int i0 = threadIdx.x; i0 < cnt; i0 += 2 * NT) {
       const int i1 = i0 + NT;
@@ -320,10 +302,6 @@ __device__ void team_run(const TeamItem &it, int rank, unsigned char *s_raw, Tea
       if (last) {
         v.ilast[n0] = I0;
         if (h1) v.ilast[n1] = I1;
-      }
-      if (pf) {
-        if (k0) prefetch_row(n0);
-        if (k1) prefetch_row(n1);
       }
       if (k0) s_own[atomicAdd(&sh.nown[par], 1)] = (int)n0;
       if (k1) s_own[atomicAdd(&sh.nown[par], 1)] = (int)n1;
@@ -737,7 +715,6 @@ __device__ void team_run(const TeamItem &it, int rank, unsigned char *s_raw, Tea
     __syncthreads();
     if (gl && sh.fail) return;
     base += K;
-    k_prev = K;
   }
   // pending currents (from the last delivery) and the state back to global memory
   for (int i = threadIdx.x; i < cnt; i += NT) {
