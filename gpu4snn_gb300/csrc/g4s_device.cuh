@@ -131,6 +131,7 @@ __device__ __forceinline__ float normal(uint64_t seed, uint64_t neuron, uint64_t
 // Q32.32 fixed point of one weight (round to nearest even).
 __device__ __forceinline__ long long wfix(float w) { return __float2ll_rn(__fmul_rn(w, kTwoP32)); }
 
+
 // Neuron parameters from one uniform r (initNeuron, gpu4snn.cu:292-317; powf(r,2) -> r*r).
 __device__ __forceinline__ float4 izh_params(uint64_t seed, int64_t i, int64_t nexc) {
   const float r = u24(philox(seed, kStreamParam, (uint64_t)i, 0, 0).x[0]);

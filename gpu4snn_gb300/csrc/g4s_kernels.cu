@@ -18,6 +18,8 @@
 // the order of the additions.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include <cstdio>
 
 #include "g4s_device.cuh"

@@ -189,6 +189,28 @@ def test_uploaded_tables_with_holes(g4s, oracle):
             compare_state(net, sim)
 
 
+@pytest.mark.parametrize("p", [0, 8])
+def test_weights_of_every_magnitude(g4s, oracle, p):
+    """Weights spread over 2^-34 .. 2^4 (tiny ones round in Q32.32, ties included), both
+    signs: the team kernel's currents and raster equal the oracle's."""
+    n, nsyn, seed = 2000, 64, 12
+    d, (idx, w) = oracle_tables(oracle, n, nsyn, seed)
+    rng = np.random.default_rng(1)
+    mag = np.ldexp(rng.uniform(1.0, 2.0, w.shape), rng.integers(-34, 4, w.shape)).astype(np.float32)
+    ties = rng.random(w.shape) < 0.2  # w 2^32 = j + 1/2 exactly
+    mag[ties] = np.ldexp(2.0 * rng.integers(0, 64, int(ties.sum())) + 1.0, -33).astype(np.float32)
+    w = np.where(rng.random(w.shape) < 0.5, -mag, mag).astype(np.float32)
+    w[idx < 0] = 0.0
+    sim = oracle.Sim(d, idx, w)
+    sim.run(60, threads=8)
+    with g4s.Network(n, nsyn, seed=seed, tables=(idx, w)) as net:
+        net.set_geometry(p, 0)
+        net.run(60, 4)
+        assert net.geometry()[0] >= 1  # the team kernel ran (tables within its exactness bound)
+        assert np.array_equal(np.stack(net.raster()), np.stack(sim.raster()))
+        compare_state(net, sim)
+
+
 def test_owner_large_network(g4s, oracle):
     """N=100,000, Nsyn=1000 (the scaled configuration) on the full GPU: many clusters."""
     n, nsyn, seed = 100_000, 1000, 2
