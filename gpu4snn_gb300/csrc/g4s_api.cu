@@ -169,6 +169,7 @@ static void free_net(g4s_net *n) {
   }
   cudaFree(v.vu);
   cudaFree(v.abcd);
+  cudaFree(v.rpar);
   cudaFree(v.acc);
   cudaFree(v.ilast);
   cudaFree(v.sstat);
@@ -265,13 +266,14 @@ static int alloc_net(const g4s_net_desc *d, g4s_net **out) {
     free_net(n);
     return cuda_error(e, "cudaMemGetInfo");
   }
-  const size_t need = N * S * 8 + N * (8 + 16 + 8 + 4 + 32) + (size_t)v.raster_cap * 4 + (size_t)cs * 32;
+  const size_t need = N * S * 8 + N * (8 + 16 + 4 + 8 + 4 + 32) + (size_t)v.raster_cap * 4 + (size_t)cs * 32;
   if (need + ((size_t)256 << 20) > free_b) {
     free_net(n);
     return set_error(G4S_ERR_NOMEM, "network needs " + std::to_string(need) + " bytes of device memory, " +
                                         std::to_string(free_b) + " free");
   }
   if ((rc = dalloc(n, &v.vu, N, "v,u")) || (rc = dalloc(n, &v.abcd, N, "a,b,c,d")) ||
+      (rc = dalloc(n, &v.rpar, N, "parameter r")) ||
       (rc = dalloc(n, &v.acc, N, "currents")) || (rc = dalloc(n, &v.ilast, N, "input current")) ||
       (rc = dalloc(n, &v.sstat, N, "spike statistics")) ||
       (rc = dalloc(n, const_cast<int **>(&v.idx), N * S, "targets")) ||

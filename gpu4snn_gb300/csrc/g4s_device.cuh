@@ -133,15 +133,22 @@ __device__ __forceinline__ long long wfix(float w) { return __float2ll_rn(__fmul
 
 
 // Neuron parameters from one uniform r (initNeuron, gpu4snn.cu:292-317; powf(r,2) -> r*r).
-__device__ __forceinline__ float4 izh_params(uint64_t seed, int64_t i, int64_t nexc) {
-  const float r = u24(philox(seed, kStreamParam, (uint64_t)i, 0, 0).x[0]);
-  if (i < nexc) {
+// a, b, c, d are a function of r and the neuron's kind, so a kernel can read r (4 bytes)
+// and recompute them instead of reading 16 bytes.
+__device__ __forceinline__ float izh_r(uint64_t seed, int64_t i) {
+  return u24(philox(seed, kStreamParam, (uint64_t)i, 0, 0).x[0]);
+}
+__device__ __forceinline__ float4 izh_abcd(float r, bool exc) {
+  if (exc) {
     const float r2 = __fmul_rn(r, r);
     return make_float4(0.02f, 0.2f, __fadd_rn(-65.0f, __fmul_rn(15.0f, r2)),
                        __fsub_rn(8.0f, __fmul_rn(6.0f, r2)));
   }
   return make_float4(__fadd_rn(0.02f, __fmul_rn(0.08f, r)), __fsub_rn(0.25f, __fmul_rn(0.05f, r)),
                      -65.0f, 2.0f);
+}
+__device__ __forceinline__ float4 izh_params(uint64_t seed, int64_t i, int64_t nexc) {
+  return izh_abcd(izh_r(seed, i), i < nexc);
 }
 
 // One 1 ms step of one neuron (stateupdate, gpu4snn.cu:376-405): I = g z + Isyn, two 0.5 ms

@@ -33,8 +33,10 @@ namespace g4s {
 __global__ void k_init_state(NetView v) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < v.n;
        i += (int64_t)gridDim.x * blockDim.x) {
-    const float4 p = izh_params(v.seed, i, v.nexc);
+    const float r = izh_r(v.seed, i);
+    const float4 p = izh_abcd(r, i < v.nexc);
     v.abcd[i] = p;
+    if (v.rpar) v.rpar[i] = r;
     v.vu[i] = make_float2(-65.0f, __fmul_rn(p.y, -65.0f));
     v.acc[i] = 0;
     v.ilast[i] = 0.0f;

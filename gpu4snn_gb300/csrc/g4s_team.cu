@@ -245,6 +245,8 @@ __device__ void team_run(const TeamItem &it, int rank, unsigned char *s_raw, Tea
   // neuron state of the slice: shared memory for the launch when it fits, else global
   float2 *vu = L.vu_sm ? s_vu : v.vu + lo;
   const float4 *abcd = L.abcd_sm ? s_abcd : v.abcd + lo;
+  const float *rp = L.abcd_sm ? nullptr : (v.rpar ? v.rpar + lo : nullptr);  // a,b,c,d recomputed from r
+  auto param = [&](int i) -> float4 { return rp ? izh_abcd(rp[i], lo + i < v.nexc) : abcd[i]; };
 
   for (int i = threadIdx.x; i < cnt; i += NT) {
     const long long q = __ldcg(v.acc + lo + i);
@@ -282,7 +284,7 @@ __device__ void team_run(const TeamItem &it, int rank, unsigned char *s_raw, Tea
       const int j1 = h1 ? i1 : i0;
       const int64_t n0 = lo + i0, n1 = lo + j1;
       float2 s0 = vu[i0], s1 = vu[j1];
-      const float4 p0 = abcd[i0], p1 = abcd[j1];
+      const float4 p0 = param(i0), p1 = param(j1);
       const long long a0 = (long long)s_a[i0] * 65536 + s_b[i0];
       const long long a1 = h1 ? (long long)s_a[i1] * 65536 + s_b[i1] : 0;
       s_a[i0] = 0;

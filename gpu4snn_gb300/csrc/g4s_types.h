@@ -43,6 +43,7 @@ struct NetView {
   float ge, gi;     // thalamic gains (5, 2) x drive scale
   float2 *vu;       // membrane potential v, recovery u
   float4 *abcd;     // a, b, c, d
+  float *rpar;      // the uniform r each neuron's a, b, c, d derive from (may be null)
   long long *acc;   // Q32.32 synaptic current, consumed and cleared by the update
   float *ilast;     // total input current of the last step of a run
   SpikeStat *sstat;
