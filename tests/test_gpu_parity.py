@@ -211,6 +211,24 @@ def test_weights_of_every_magnitude(g4s, oracle, p):
         compare_state(net, sim)
 
 
+def test_large_steps_dense_list(g4s, oracle):
+    """Steps with more than 4096 spikes (the ids go through the dense global list instead of
+    the shared-memory window) and ranks with more than 31 spikes (ids beyond the record
+    lines): N=200,000 under a strong drive, against the oracle."""
+    n, nsyn, seed, drive, steps = 200_000, 1000, 4, 2.0, 60
+    d, (idx, w) = oracle_tables(oracle, n, nsyn, seed)
+    d = oracle.make_desc(n, nsyn, seed, drive_scale=drive)
+    sim = oracle.Sim(d, idx, w)
+    sim.run(steps, threads=16)
+    assert sim.counts().max() > 4096  # the dense-list path runs
+    with g4s.Network(n, nsyn, seed=seed, drive_scale=drive) as net:
+        assert net.geometry()[0] > 1
+        net.run(steps, 4)
+        assert np.array_equal(net.counts(), sim.counts())
+        assert np.array_equal(np.stack(net.raster()), np.stack(sim.raster()))
+        compare_state(net, sim)
+
+
 def test_owner_large_network(g4s, oracle):
     """N=100,000, Nsyn=1000 (the scaled configuration) on the full GPU: many clusters."""
     n, nsyn, seed = 100_000, 1000, 2
