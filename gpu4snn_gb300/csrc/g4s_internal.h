@@ -55,7 +55,7 @@ constexpr int kFlatMax = 8192;                 // synapses of a step a rank deli
 constexpr int64_t kFlatSlice = 4096;           // ... on slices up to this size
 // Spike records of a multi-CTA team: per rank and step parity kRecLines lines of 16
 // tagged 64-bit words (count, then up to 16 kRecLines - 1 ids); readers fetch the second
-// line of a rank only if it had more than 15 spikes in the previous step.
+// line of a rank only if it had enough spikes in the previous step (g4s_team.cu).
 constexpr int kRecLines = 2;
 constexpr int kRecWords = 16;
 

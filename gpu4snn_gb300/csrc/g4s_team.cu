@@ -29,22 +29,30 @@
 //             reader that sees the tag it expects needs no fence to trust the payload:
 //             two 128-byte record lines (count and 31 ids), further ids in a per-rank
 //             overflow list.  Every rank reads, in one pass, line 0 of every rank and
-//             line 1 of the ranks that had more than 15 spikes in the previous step
-//             (16-byte slots, polled until their tags are current, with a time limit), so
-//             the records double as the team barrier; ids beyond the lines read are
-//             polled word by word.  The step's ids are staged in shared memory (in
-//             windows when they do not fit).  Records are cleared before each launch.
-//             Two record sets (by step parity) suffice: a rank writes step t+2's words
-//             only after every rank has published step t+1, i.e. finished reading step t.
+//             line 1 of the ranks that had more than kLine1After spikes in the previous
+//             step (16-byte slots, polled until their tags are current, with a time
+//             limit), so the records double as the team barrier; ids beyond the lines
+//             read are polled word by word.  The step's ids are staged in shared memory;
+//             a step with more ids than the window writes a dense tagged list in global
+//             memory instead, read directly by the delivery.  Records are cleared before
+//             each launch.  Two record sets (by step parity) suffice: a rank writes step
+//             t+2's words only after every rank has published step t+1, i.e. finished
+//             reading step t.
 //   delivery  one-CTA team: whole spiking rows, 128-bit loads, flat over all threads.
-//             Larger team: every rank streams, for every spike, the segment of the
-//             spiking row whose targets fall in its slice (rows are sorted by target and
-//             a per-row offset table gives the segment): a warp takes 32 spikes, scans
-//             their segment lengths and walks the concatenated segments, eight synapses
-//             per lane in flight.  Each weight goes into the rank's own shared memory.
+//             Larger team: every rank reads, for every spike, the segment of the spiking
+//             row whose targets fall in its slice (rows are sorted by target and a per-row
+//             offset table gives the segment).  Flat mapping (at least kFlatMinSpikes
+//             staged spikes, at most kFlatMax synapses for the rank): the segment bounds
+//             of all spikes at once, a block scan, every synapse of the concatenation
+//             mapped to its spike in shared memory, and thread i walks synapses i, i+NT,
+//             ... with eight reads in flight.  Run mapping (otherwise): a warp takes 32
+//             spikes, scans their segment lengths and walks the concatenated segments,
+//             eight synapses per lane in flight.  Each weight goes into the rank's own
+//             shared memory.
 //   tail      the raster and the spike statistics of this rank's spikes, and the next
 //             step's drive, handed out in chunks of 32 neurons to warps as they finish
-//             delivering.
+//             delivering (the flat mapping computes each thread's own neuron's drive
+//             while its reads are in flight).
 //   The raster records the spike ids of every step while its buffer has room.
 #include <cuda_runtime.h>
 
