@@ -56,15 +56,26 @@ struct TeamLaunch {
   TeamItem *d_items = nullptr, *h_items = nullptr;
   int2 *d_slots = nullptr, *h_slots = nullptr;
   int *d_ctl = nullptr, *h_ctl = nullptr;  // [0] slot count, [1] queue head
+  int *h_status = nullptr;                 // per item: status word, team error word
   int cap_items = 0, cap_slots = 0;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
+  // the round as a CUDA graph, replayed while its shape (networks, teams, buffers) holds
+  cudaGraphExec_t exec = nullptr;
+  std::vector<uint64_t> sig;
+  void drop_graph() {
+    if (exec) cudaGraphExecDestroy(exec);
+    exec = nullptr;
+    sig.clear();
+  }
   void release() {
+    drop_graph();
     cudaFree(d_items);
     cudaFree(d_slots);
     cudaFree(d_ctl);
     cudaFreeHost(h_items);
     cudaFreeHost(h_slots);
     cudaFreeHost(h_ctl);
+    cudaFreeHost(h_status);
     if (e0) cudaEventDestroy(e0);
     if (e1) cudaEventDestroy(e1);
     *this = TeamLaunch{};
@@ -75,15 +86,20 @@ struct TeamLaunch {
     if (!d_ctl && (cudaMalloc((void **)&d_ctl, 16) != cudaSuccess || cudaMallocHost((void **)&h_ctl, 16) != cudaSuccess))
       return set_error(G4S_ERR_NOMEM, "team launch control words");
     if (items > cap_items) {
+      drop_graph();
       cudaFree(d_items);
       cudaFreeHost(h_items);
+      cudaFreeHost(h_status);
       d_items = h_items = nullptr;
+      h_status = nullptr;
       if (cudaMalloc((void **)&d_items, sizeof(TeamItem) * items) != cudaSuccess ||
-          cudaMallocHost((void **)&h_items, sizeof(TeamItem) * items) != cudaSuccess)
+          cudaMallocHost((void **)&h_items, sizeof(TeamItem) * items) != cudaSuccess ||
+          cudaMallocHost((void **)&h_status, sizeof(int) * 2 * items) != cudaSuccess)
         return set_error(G4S_ERR_NOMEM, "team items");
       cap_items = items;
     }
     if (slots > cap_slots) {
+      drop_graph();
       cudaFree(d_slots);
       cudaFreeHost(h_slots);
       d_slots = h_slots = nullptr;
@@ -119,6 +135,7 @@ struct g4s_net {
   int64_t chunk_legacy = 0;  // steps per chunk of the other kernels (raster = spike list)
   int64_t t_abs = 0;
   uint32_t tag_next = 0;  // record tags of the team kernel: never repeated for this handle's lists
+  uint64_t serial = 0;    // creation number, unique in the process (keys the captured rounds)
   unsigned long long barrier_ns = 2000000000ull;
   size_t device_bytes = 0;
   // pinned staging of one chunk
@@ -167,6 +184,7 @@ static void free_net(g4s_net *n) {
     raster_close(n->rstream);
     n->rstream = nullptr;
   }
+  n->launch.release();  // its captured round refers to the buffers below
   cudaFree(v.vu);
   cudaFree(v.abcd);
   cudaFree(v.rpar);
@@ -184,7 +202,6 @@ static void free_net(g4s_net *n) {
   cudaFree(n->d_stats);
   cudaFree(n->seg);
   cudaFree(n->list);
-  n->launch.release();
   cudaFreeHost(n->h_counts);
   cudaFreeHost(n->h_base);
   cudaFreeHost(n->h_stamps);
@@ -238,6 +255,8 @@ static int alloc_net(const g4s_net_desc *d, g4s_net **out) {
   if (rc) return rc;
   g4s_net *n = new (std::nothrow) g4s_net;
   if (!n) return set_error(G4S_ERR_NOMEM, "host allocation");
+  static std::atomic<uint64_t> next_serial{1};
+  n->serial = next_serial++;
   n->desc = *d;
   NetView &v = n->v;
   v.n = d->n;
@@ -311,11 +330,18 @@ static int alloc_net(const g4s_net_desc *d, g4s_net **out) {
   return G4S_OK;
 }
 
+static int status_rc(int st, int bar, const char *what);
+
 static int check_status(g4s_net *n, const char *what) {
   int st = 0, bar = 0;
   G4S_CUDA(cudaMemcpyAsync(&st, n->v.status, sizeof(int), cudaMemcpyDeviceToHost, n->stream));
   G4S_CUDA(cudaMemcpyAsync(&bar, &n->gs->error, sizeof(int), cudaMemcpyDeviceToHost, n->stream));
   G4S_CUDA(cudaStreamSynchronize(n->stream));
+  return status_rc(st, bar, what);
+}
+
+// The device's status word and a team's error word as a G4S status.
+static int status_rc(int st, int bar, const char *what) {
   if (bar == kErrTimeoutCode) return set_error(G4S_ERR_TIMEOUT, std::string(what) + ": grid barrier timed out");
   if (st == kErrOverflowCode) return set_error(G4S_ERR_OVERFLOW, std::string(what) + ": raster overflow");
   if (st == kErrConnCode) return set_error(G4S_ERR_INVALID, std::string(what) + ": connectivity draws exhausted");
@@ -609,6 +635,15 @@ static int absorb_chunk(g4s_net *n, int cs, int64_t *spikes) {
   return G4S_OK;
 }
 
+// The same after a team round, whose graph copied the counts, offsets and stamps.
+static int absorb_raster(g4s_net *n, int cs, int64_t *spikes) {
+  int rc = chunk_copy_raster(n, cs, n->stream);
+  if (rc) return rc;
+  G4S_CUDA(cudaStreamSynchronize(n->stream));
+  chunk_finish(n, cs, spikes);
+  return G4S_OK;
+}
+
 // ---------------------------------------------------------------------------------------
 // One launch of the team kernel over several networks (a "round"): network i advances
 // steps[i] steps (at most its chunk length).  Multi-CTA teams are queued first, then the
@@ -635,6 +670,11 @@ static int team_round(g4s_net *const *nets, const int *steps, const bool *last, 
   });
   int rc = L.reserve(count, nslots);
   if (rc) return rc;
+  int gmax = 0;
+  G4S_CUDA(team_max_blocks(smem, &gmax));  // also raises the kernel's shared-memory ceiling
+  if (gmax < maxteam) return set_error(G4S_ERR_CUDA, "team larger than the co-resident grid");
+  const int grid = std::min(nslots, gmax);
+  // this round's descriptors, in pinned host memory the graph copies from
   int k = 0;
   for (int i : order) {
     g4s_net *n = nets[i];
@@ -658,33 +698,78 @@ static int team_round(g4s_net *const *nets, const int *steps, const bool *last, 
     it.tag0 = n->tag_next;
     n->tag_next += (uint32_t)steps[i];
     for (int r = 0; r < n->team_p; ++r) L.h_slots[k++] = make_int2(i, r);
-    G4S_CUDA(cudaMemsetAsync(n->v.counts, 0, (size_t)steps[i] * sizeof(int), s));
-    G4S_CUDA(cudaMemsetAsync(n->v.stamps, 0, ((size_t)steps[i] * 2 + 2) * 8, s));
-    G4S_CUDA(cudaMemsetAsync(n->v.status, 0, sizeof(int), s));
-    // error word and the team's spike records (two sets of kRecLines 128-byte lines per rank)
-    G4S_CUDA(cudaMemsetAsync(n->gs, 0, sizeof(GridSync) * (1 + 2 * (size_t)n->team_p * kRecLines), s));
   }
   for (int i = 0; i < count; ++i)
     if (steps[i] <= 0) L.h_items[i].steps = 0;
   L.h_ctl[0] = nslots;
   L.h_ctl[1] = 0;
-  G4S_CUDA(cudaMemcpyAsync(L.d_items, L.h_items, sizeof(TeamItem) * count, cudaMemcpyHostToDevice, s));
-  G4S_CUDA(cudaMemcpyAsync(L.d_slots, L.h_slots, sizeof(int2) * nslots, cudaMemcpyHostToDevice, s));
-  G4S_CUDA(cudaMemcpyAsync(L.d_ctl, L.h_ctl, 8, cudaMemcpyHostToDevice, s));
-  int gmax = 0;
-  G4S_CUDA(team_max_blocks(smem, &gmax));
-  if (gmax < maxteam) return set_error(G4S_ERR_CUDA, "team larger than the co-resident grid");
-  const int grid = std::min(nslots, gmax);
-  G4S_CUDA(cudaEventRecord(L.e0, s));
-  G4S_CUDA(launch_team(L.d_items, L.d_slots, L.d_ctl, L.d_ctl + 1, grid, smem, limit_ns, stall, s));
-  G4S_CUDA(cudaEventRecord(L.e1, s));
-  G4S_CUDA(cudaEventSynchronize(L.e1));
+  // The round's graph: clear the networks' per-chunk arrays, error words and spike records,
+  // upload the descriptors, the persistent launch between two timing events, and copy
+  // back each network's per-step counts, offsets and stamps and its status words.  Its
+  // shape depends only on which networks run, their teams and chunk lengths, and the
+  // launch parameters; the descriptors' contents are read from pinned memory at replay.
+  // A graph must not outlive the buffers it copies to and from: a network freed and another
+  // created in its place (often at the same device and pinned host addresses) gets a new
+  // graph, so the key holds each network's creation number as well as its addresses.
+  auto u = [](const void *p) { return (uint64_t)(uintptr_t)p; };
+  std::vector<uint64_t> sig = {(uint64_t)count, (uint64_t)nslots, (uint64_t)grid, (uint64_t)smem, limit_ns,
+                               (uint64_t)stall, u(L.d_items), u(L.d_slots), u(L.d_ctl), u(L.h_items),
+                               u(L.h_slots), u(L.h_ctl), u(L.h_status), u(L.e0), u(L.e1)};
+  for (int i : order) {
+    const g4s_net *n = nets[i];
+    for (uint64_t x : {(uint64_t)i, n->serial, (uint64_t)n->team_p, (uint64_t)n->chunk_steps, u(n->v.counts), u(n->v.stamps),
+                       u(n->v.status), u(n->gs), u(n->v.base), u(n->h_counts), u(n->h_base), u(n->h_stamps)})
+      sig.push_back(x);
+  }
+  if (!L.exec || sig != L.sig) {
+    L.drop_graph();
+    G4S_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = cudaSuccess;
+    for (int i : order) {
+      const g4s_net *n = nets[i];
+      const size_t cs = (size_t)n->chunk_steps;
+      if (e == cudaSuccess) e = cudaMemsetAsync(n->v.counts, 0, cs * sizeof(int), s);
+      if (e == cudaSuccess) e = cudaMemsetAsync(n->v.stamps, 0, (cs * 2 + 2) * 8, s);
+      if (e == cudaSuccess) e = cudaMemsetAsync(n->v.status, 0, sizeof(int), s);
+      // error word and the team's spike records (two sets of kRecLines 128-byte lines per rank)
+      if (e == cudaSuccess) e = cudaMemsetAsync(n->gs, 0, sizeof(GridSync) * (1 + 2 * (size_t)n->team_p * kRecLines), s);
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(L.d_items, L.h_items, sizeof(TeamItem) * count, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(L.d_slots, L.h_slots, sizeof(int2) * nslots, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(L.d_ctl, L.h_ctl, 8, cudaMemcpyHostToDevice, s);
+    // (external records: the graph records the events at every replay)
+    if (e == cudaSuccess) e = cudaEventRecordWithFlags(L.e0, s, cudaEventRecordExternal);
+    if (e == cudaSuccess) e = launch_team(L.d_items, L.d_slots, L.d_ctl, L.d_ctl + 1, grid, smem, limit_ns, stall, s);
+    if (e == cudaSuccess) e = cudaEventRecordWithFlags(L.e1, s, cudaEventRecordExternal);
+    for (int i : order) {
+      const g4s_net *n = nets[i];
+      const size_t cs = (size_t)n->chunk_steps;
+      if (e == cudaSuccess) e = cudaMemcpyAsync(n->h_counts, n->v.counts, cs * 4, cudaMemcpyDeviceToHost, s);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(n->h_base, n->v.base, cs * 8, cudaMemcpyDeviceToHost, s);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(n->h_stamps, n->v.stamps, cs * 16, cudaMemcpyDeviceToHost, s);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(L.h_status + 2 * i, n->v.status, sizeof(int), cudaMemcpyDeviceToHost, s);
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(L.h_status + 2 * i + 1, &n->gs->error, sizeof(int), cudaMemcpyDeviceToHost, s);
+    }
+    cudaGraph_t g = nullptr;
+    const cudaError_t e_end = cudaStreamEndCapture(s, &g);
+    if (e == cudaSuccess) e = e_end;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&L.exec, g, 0);
+    if (g) cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+      L.exec = nullptr;
+      return cuda_error(e, "capturing the team round as a CUDA graph");
+    }
+    L.sig = sig;
+  }
+  G4S_CUDA(cudaGraphLaunch(L.exec, s));
+  G4S_CUDA(cudaStreamSynchronize(s));
   float ms = 0.0f;
   G4S_CUDA(cudaEventElapsedTime(&ms, L.e0, L.e1));
   *kernel_ms += ms;
   *launches += 1;
   for (int i : order) {
-    rc = check_status(nets[i], "team step kernel");
+    rc = status_rc(L.h_status[2 * i], L.h_status[2 * i + 1], "team step kernel");
     if (rc) return rc;
   }
   return G4S_OK;
@@ -740,7 +825,8 @@ static int run_net(g4s_net *n, int32_t steps, int32_t alg_in) {
       kernel_ms += kms;
     }
     int64_t chunk_spikes = 0;
-    int rc = absorb_chunk(n, cs, &chunk_spikes);
+    // (a team round's graph already copied the per-step counts, offsets and stamps back)
+    int rc = team ? absorb_raster(n, cs, &chunk_spikes) : absorb_chunk(n, cs, &chunk_spikes);
     if (rc) return rc;
     spikes += chunk_spikes;
     remaining -= cs;
@@ -795,9 +881,6 @@ static int run_nets(g4s_net *const *nets, const int32_t *steps, int count, doubl
     if (!any) break;
     int rc = team_round(nets, cs.data(), last.get(), count, L, s, nets[0]->barrier_ns, 0, &kms, &nl);
     if (rc) return rc;
-    for (int i = 0; i < count; ++i)
-      if (cs[i] > 0 && (rc = chunk_copy_meta(nets[i], cs[i], s))) return rc;
-    G4S_CUDA(cudaStreamSynchronize(s));
     for (int i = 0; i < count; ++i)
       if (cs[i] > 0 && (rc = chunk_copy_raster(nets[i], cs[i], s))) return rc;
     G4S_CUDA(cudaStreamSynchronize(s));

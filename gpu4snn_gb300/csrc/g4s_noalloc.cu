@@ -68,6 +68,8 @@ static int scratch_address(unsigned char **out) {
     void *p = nullptr;
     e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess || !p) return cuda_error(e, "cudaGetSymbolAddress of the no-alloc scratch");
+    // once per device, outside any stream capture of the caller's launches
+    if ((e = team_smem_ceiling()) != cudaSuccess) return cuda_error(e, "team kernel shared-memory ceiling");
     g_scratch_dev[dev] = p;
   }
   *out = static_cast<unsigned char *>(g_scratch_dev[dev]);

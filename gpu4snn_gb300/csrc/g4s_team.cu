@@ -771,8 +771,16 @@ size_t team_smem(int64_t rc, int team) {
   return bytes > kTeamSmemLimit ? 0 : (bytes < 16 ? 16 : bytes);
 }
 
+// The kernel's shared-memory ceiling is always the largest layout's (every team layout
+// stays under it), so host threads that launch teams of different sizes never lower it
+// under one another, and a captured launch needs no attribute call.
+cudaError_t team_smem_ceiling() {
+  return cudaFuncSetAttribute(k_team<kTeamNT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTeamSmemLimit);
+}
+
 cudaError_t team_max_blocks(size_t smem, int *out) {
-  cudaError_t e = cudaFuncSetAttribute(k_team<kTeamNT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (smem > kTeamSmemLimit) return cudaErrorInvalidValue;
+  cudaError_t e = team_smem_ceiling();
   if (e != cudaSuccess) return e;
   int occ = 0;
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_team<kTeamNT>, kTeamNT, smem);
@@ -786,8 +794,7 @@ cudaError_t team_max_blocks(size_t smem, int *out) {
 
 cudaError_t launch_team(const TeamItem *items, const int2 *slots, const int *nslots, int *slot_head, int grid,
                         size_t smem, unsigned long long limit_ns, int stall, cudaStream_t s) {
-  cudaError_t e = cudaFuncSetAttribute(k_team<kTeamNT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
+  if (smem > kTeamSmemLimit) return cudaErrorInvalidValue;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)grid);
   cfg.blockDim = dim3(kTeamNT);
