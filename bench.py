@@ -46,10 +46,11 @@ WORKLOADS = {
     "n300k": (300_000, 1000, 50, 1.0, 6),  # profiling case for large-N delivery: 2.4 GB of tables
 }
 # algorithmic bytes: delivery = spikes x Nsyn x (4 B target + 4 B weight) and the spike
-# statistics (32 B read + 32 B written per spike); the neuron state (v,u read+write 16 B,
-# a,b,c,d 16 B, current 8 B per neuron and step) only when it is not kept on chip: the team
-# kernel holds slices of up to RESIDENT_SLICE neurons in shared memory for a whole launch
-UPDATE_BYTES_PER_NEURON = 40
+# statistics (32 B read + 32 B written per spike); the neuron state (v,u read + write 16 B
+# and the parameter r 4 B per neuron and step, a,b,c,d being recomputed from r; the currents
+# stay in shared memory) only when it is not kept on chip: the team kernel holds slices of
+# up to RESIDENT_SLICE neurons in shared memory for a whole launch
+UPDATE_BYTES_PER_NEURON = 20
 STAT_BYTES_PER_SPIKE = 64
 RESIDENT_SLICE = 2048
 

@@ -160,6 +160,7 @@ struct g4s_net {
   bool team_ready = false;
   bool team_batch = false;  // geometry planned for a multi-network batch
   bool team_ok = true;
+  bool pair_ready = false;  // the interleaved rows match the tables
   unsigned long long *list = nullptr;
   uint16_t *seg = nullptr;
   size_t seg_bytes = 0;
@@ -185,6 +186,7 @@ static void free_net(g4s_net *n) {
     n->rstream = nullptr;
   }
   n->launch.release();  // its captured round refers to the buffers below
+  cudaFree(const_cast<int2 *>(v.pair));
   cudaFree(v.vu);
   cudaFree(v.abcd);
   cudaFree(v.rpar);
@@ -514,6 +516,22 @@ static int prepare_team(g4s_net *n, bool batch = false) {
     n->team_ok = false;
     return G4S_OK;
   }
+  // the interleaved rows of the team kernel's segment reads: optional (without them, as
+  // when the device has no room left for them, the kernel reads the separate arrays)
+  if (!n->v.pair) {
+    const size_t bytes = (size_t)n->v.n * (size_t)n->v.stride * sizeof(int2);
+    if (!g_fail_next_alloc.exchange(0) && cudaMalloc((void **)&n->v.pair, bytes) == cudaSuccess) {
+      n->device_bytes += bytes;
+      n->pair_ready = false;
+    } else {
+      (void)cudaGetLastError();
+      n->v.pair = nullptr;
+    }
+  }
+  if (n->v.pair && !n->pair_ready) {
+    G4S_CUDA(launch_pairs(n->v, n->stream));
+    n->pair_ready = true;
+  }
   if (!n->list) {
     cudaError_t e = cudaMalloc((void **)&n->list, (size_t)n->v.n * 4 * sizeof(unsigned long long));
     if (e != cudaSuccess) return cuda_error(e, "spike lists");
@@ -551,6 +569,7 @@ static int prepare_team(g4s_net *n, bool batch = false) {
 static int finish_tables(g4s_net *n) {
   G4S_CUDA(launch_sort_rows(n->v, n->stream));
   n->team_ready = false;
+  n->pair_ready = false;
   unsigned *cnt = nullptr;
   unsigned long long *mag = nullptr, *out = nullptr;
   cudaError_t e = cudaMalloc((void **)&cnt, (size_t)n->v.n * 4);
@@ -670,6 +689,8 @@ static int team_round(g4s_net *const *nets, const int *steps, const bool *last, 
   });
   int rc = L.reserve(count, nslots);
   if (rc) return rc;
+  bool pair = true;  // every network of the round has its interleaved rows
+  for (int i : order) pair = pair && nets[i]->v.pair != nullptr;
   int gmax = 0;
   G4S_CUDA(team_max_blocks(smem, &gmax));  // also raises the kernel's shared-memory ceiling
   if (gmax < maxteam) return set_error(G4S_ERR_CUDA, "team larger than the co-resident grid");
@@ -713,7 +734,7 @@ static int team_round(g4s_net *const *nets, const int *steps, const bool *last, 
   // graph, so the key holds each network's creation number as well as its addresses.
   auto u = [](const void *p) { return (uint64_t)(uintptr_t)p; };
   std::vector<uint64_t> sig = {(uint64_t)count, (uint64_t)nslots, (uint64_t)grid, (uint64_t)smem, limit_ns,
-                               (uint64_t)stall, u(L.d_items), u(L.d_slots), u(L.d_ctl), u(L.h_items),
+                               (uint64_t)stall, (uint64_t)pair, u(L.d_items), u(L.d_slots), u(L.d_ctl), u(L.h_items),
                                u(L.h_slots), u(L.h_ctl), u(L.h_status), u(L.e0), u(L.e1)};
   for (int i : order) {
     const g4s_net *n = nets[i];
@@ -739,7 +760,7 @@ static int team_round(g4s_net *const *nets, const int *steps, const bool *last, 
     if (e == cudaSuccess) e = cudaMemcpyAsync(L.d_ctl, L.h_ctl, 8, cudaMemcpyHostToDevice, s);
     // (external records: the graph records the events at every replay)
     if (e == cudaSuccess) e = cudaEventRecordWithFlags(L.e0, s, cudaEventRecordExternal);
-    if (e == cudaSuccess) e = launch_team(L.d_items, L.d_slots, L.d_ctl, L.d_ctl + 1, grid, smem, limit_ns, stall, s);
+    if (e == cudaSuccess) e = launch_team(L.d_items, L.d_slots, L.d_ctl, L.d_ctl + 1, grid, smem, limit_ns, stall, s, pair);
     if (e == cudaSuccess) e = cudaEventRecordWithFlags(L.e1, s, cudaEventRecordExternal);
     for (int i : order) {
       const g4s_net *n = nets[i];

@@ -130,8 +130,11 @@ cudaError_t launch_inbound(const NetView &v, unsigned *cnt, unsigned long long *
                            cudaStream_t s);
 // team_max_blocks also raises the kernel's shared-memory ceiling: call it once before the
 // first launch_team (which may then be captured in a CUDA graph)
+// pair: the tables are read from v.pair (interleaved rows) instead of v.idx and v.w
 cudaError_t launch_team(const TeamItem *items, const int2 *slots, const int *nslots, int *slot_head, int grid,
-                        size_t smem, unsigned long long limit_ns, int stall, cudaStream_t s);
+                        size_t smem, unsigned long long limit_ns, int stall, cudaStream_t s, bool pair);
+// v.pair <- the rows of v.idx and v.w interleaved (after every change of the tables)
+cudaError_t launch_pairs(const NetView &v, cudaStream_t s);
 cudaError_t team_max_blocks(size_t smem, int *out);
 cudaError_t team_smem_ceiling();  // the part of team_max_blocks that launch_team needs
 // shared memory of one rank of a team of `team` CTAs with `rc` neurons each (0: does not fit)

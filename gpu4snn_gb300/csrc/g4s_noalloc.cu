@@ -160,7 +160,7 @@ extern "C" int g4s_run_noalloc(const g4s_dev_net *d, int64_t t_abs0, int32_t ste
   if (e == cudaSuccess) e = cudaMemcpyAsync(item, &h, sizeof h, cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess && team > 1) e = launch_segoff(v, team, rc, seg, s);
   if (e == cudaSuccess)
-    e = launch_team(item, slots, ctl, ctl + 1, team, team_smem(rc, team), 2000000000ull, 0, s);
+    e = launch_team(item, slots, ctl, ctl + 1, team, team_smem(rc, team), 2000000000ull, 0, s, false);
   if (e == cudaSuccess && d_status) e = cudaMemcpyAsync(d_status, &sync->error, sizeof(int32_t), cudaMemcpyDeviceToDevice, s);
   if (e != cudaSuccess) return cuda_error(e, "g4s_run_noalloc launch");
   return G4S_OK;

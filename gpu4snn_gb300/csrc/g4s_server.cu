@@ -52,8 +52,9 @@ struct Request {
 int64_t estimate_bytes(const g4s_request &r, int32_t quantum) {
   const int64_t stride = ((int64_t)r.nsyn + 3) / 4 * 4;
   const int64_t raster = r.record_raster ? 4 * r.n * (int64_t)quantum : ((int64_t)64 << 20);
-  // tables, neuron state and statistics, spike lists, raster, per-step arrays
-  return r.n * stride * 8 + r.n * (8 + 16 + 4 + 8 + 4 + 32 + 32 + 4) + raster + 16384 * 28 + ((int64_t)1 << 20);
+  // tables (and their interleaved copy), neuron state and statistics, spike lists, raster,
+  // per-step arrays
+  return r.n * stride * 16 + r.n * (8 + 16 + 4 + 8 + 4 + 32 + 32 + 4) + raster + 16384 * 28 + ((int64_t)1 << 20);
 }
 
 }  // namespace

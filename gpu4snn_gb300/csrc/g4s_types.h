@@ -49,6 +49,8 @@ struct NetView {
   SpikeStat *sstat;
   const int *idx;   // [n][stride] targets
   const float *w;   // [n][stride] weights
+  const int2 *pair;  // [n][stride] the same rows interleaved (target, weight bits): one
+                     // contiguous run per segment for the team kernel (may be null)
   int *raster;      // spike ids of the current chunk, step after step
   int64_t raster_cap;
   int *counts;      // spikes per step of the current chunk

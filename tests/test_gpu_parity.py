@@ -243,6 +243,31 @@ def test_owner_large_network(g4s, oracle):
         compare_state(net, sim)
 
 
+@pytest.mark.parametrize("p,delivery", [(8, 0), (8, 1), (0, 0)])
+def test_team_without_interleaved_rows(g4s, p, delivery):
+    """The team kernel's segment reads come from the interleaved (target, weight) rows; a
+    network that finds no room for them (an allocation failure injected on the host) runs
+    on the separate target and weight arrays with identical results.  8 CTAs: 6,250-neuron
+    slices, segment runs (0) or one lane per spike (1); the default geometry adds the flat
+    mapping."""
+    from gpu4snn_gb300 import _lib
+    n, nsyn, seed, steps = 50_000, 1000, 41, 300
+    with g4s.Network(n, nsyn, seed=seed, drive_scale=1.5) as a, \
+            g4s.Network(n, nsyn, seed=seed, drive_scale=1.5) as b:
+        a.set_geometry(p, delivery)
+        b.set_geometry(p, delivery)
+        a.run(steps, 4)
+        b.inject_fault(_lib.FAULT_ALLOC)  # b's first team run finds no room for the pairs
+        b.run(steps, 4)
+        assert a.info().device_bytes - b.info().device_bytes == n * nsyn * 8
+        assert a.counts().sum() > steps * 100
+        assert np.array_equal(np.stack(a.raster()), np.stack(b.raster()))
+        sa, sb = a.state(), b.state()
+        for k in ("v", "u"):
+            assert np.array_equal(sa[k].view(np.uint32), sb[k].view(np.uint32)), k
+        assert np.array_equal(a.currents(), b.currents())
+
+
 def test_batch_matches_individual_runs(g4s, oracle):
     """Networks of uneven size, fan-out, seed and drive advanced together by the team
     kernel give exactly the results of each run alone (and of the oracle)."""
