@@ -368,7 +368,9 @@ cudaError_t launch_conngen(const NetView &v, int self_loops, cudaStream_t s) {
   if (wpb < 1) wpb = 1;
   const size_t smem = per_warp * wpb;
   if (smem > 200 * 1024) return cudaErrorInvalidValue;
-  cudaError_t e = cudaFuncSetAttribute(k_conngen, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  // one ceiling for every network (concurrent host threads generating tables of different
+  // fan-outs must not lower it under one another's launch)
+  cudaError_t e = cudaFuncSetAttribute(k_conngen, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
   if (e != cudaSuccess) return e;
   const uint64_t range = self_loops ? (uint64_t)v.n : (uint64_t)(v.n - 1);
   // generous cap on draw blocks (a full row needs about range * ln(range) draws)

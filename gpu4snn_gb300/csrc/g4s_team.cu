@@ -842,7 +842,9 @@ cudaError_t launch_sort_rows(const NetView &v, cudaStream_t s) {
   while (p2 < v.stride) p2 <<= 1;
   const size_t smem = (size_t)p2 * 8;
   if (smem > 200 * 1024) return cudaErrorInvalidValue;
-  cudaError_t e = cudaFuncSetAttribute(k_sort_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  // the ceiling is the same for every network, so that host threads sorting rows of
+  // different lengths never lower it under one another's launch
+  cudaError_t e = cudaFuncSetAttribute(k_sort_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
   if (e != cudaSuccess) return e;
   const int nt = p2 >= 4096 ? 1024 : (p2 >= 1024 ? 256 : 128);
   int occ = 0;
