@@ -418,6 +418,18 @@ int conn_glibc_host(unsigned seed, int32_t n, int32_t nsyn, int32_t stride, int3
   }
   return G4S_OK;
 }
+
+double net_recent_step_ms(const g4s_net *n, int64_t k) {
+  double sum = 0.0;
+  int64_t used = 0;
+  for (int64_t i = (int64_t)n->step_ms.size() - 1; i >= 0 && k > 0; --i, --k)
+    if (n->step_ms[(size_t)i] > 0.0f) {  // (the last step of a launch has no successor stamp)
+      sum += n->step_ms[(size_t)i];
+      ++used;
+    }
+  return used ? sum / (double)used : 0.0;
+}
+
 }  // namespace g4s
 
 // ---------------------------------------------------------------------------------------

@@ -8,6 +8,8 @@
 
 #include "g4s_types.h"
 
+struct g4s_net;  // the handle of the C ABI
+
 namespace g4s {
 
 // Propagation schemes, numbered as the reference's `dynamic` (gpu4snn.cu:1083).
@@ -136,6 +138,8 @@ cudaError_t launch_team(const TeamItem *items, const int2 *slots, const int *nsl
 // v.pair <- the rows of v.idx and v.w interleaved (after every change of the tables)
 cudaError_t launch_pairs(const NetView &v, cudaStream_t s);
 cudaError_t team_max_blocks(size_t smem, int *out);
+// mean duration in ms of the last k simulated steps of a handle with a step time (0: none)
+double net_recent_step_ms(const g4s_net *n, int64_t k);
 cudaError_t team_smem_ceiling();  // the part of team_max_blocks that launch_team needs
 // shared memory of one rank of a team of `team` CTAs with `rc` neurons each (0: does not fit)
 size_t team_smem(int64_t rc, int team);

@@ -3,8 +3,10 @@
 // Requests (network size, fan-out, steps, seed, drive) are submitted from any thread.  An
 // admission thread turns queued requests into device-resident networks (tables generated
 // on the GPU, on the network's own stream) while their estimated device bytes fit the
-// memory budget; a round thread advances every resident request together, each by up to
-// `quantum` steps, in one persistent launch of the SKL team kernel (g4s_nets_run).  A
+// memory budget; a round thread advances every resident request together in one
+// persistent launch of the SKL team kernel (g4s_nets_run): `quantum` steps in its first
+// round, then as many as the median resident request runs in `quantum` steps (from the
+// measured per-step times), so that the round's teams finish together.  A
 // request that has run all its steps leaves at the end of its round: its raster, counts,
 // final state and statistics are copied to the host, its device memory is freed, and
 // requests admitted meanwhile join the next round.  So arrivals overlap on the GPU with
@@ -39,6 +41,7 @@ struct Request {
   g4s_net *net = nullptr;
   int64_t est_bytes = 0;
   int32_t remaining = 0;
+  double step_ms = 0.0;  // measured per-step time in the last round (0: not yet run)
   Clock::time_point t_submit, t_admit, t_done;
   // results, on the host once the request is done
   int status = 0;
@@ -48,6 +51,9 @@ struct Request {
   int64_t spikes = 0;
   double rate_hz = 0, isi_cv = 0;
 };
+
+// most steps a request without a recorded raster advances in one round (its chunk length)
+constexpr int64_t kRoundMaxSteps = 16384;
 
 int64_t estimate_bytes(const g4s_request &r, int32_t quantum) {
   const int64_t stride = ((int64_t)r.nsyn + 3) / 4 * 4;
@@ -160,11 +166,28 @@ static void round_loop(g4s_server *s) {
         s->admitted.pop_front();
       }
     }
+    // Time-balanced rounds: a request that has run before advances by as many steps as
+    // the median measured request does in `quantum` steps, so that the teams of a round
+    // finish together instead of the fast ones idling while the slowest runs its quantum
+    // (capped by the request's chunk: the quantum when its raster is recorded).
+    std::vector<double> seen;
+    for (auto &r : active)
+      if (r->step_ms > 0.0) seen.push_back(r->step_ms);
+    double target_ms = 0.0;
+    if (!seen.empty()) {
+      std::nth_element(seen.begin(), seen.begin() + seen.size() / 2, seen.end());
+      target_ms = seen[seen.size() / 2] * s->quantum;
+    }
     std::vector<g4s_net *> nets;
     std::vector<int32_t> steps;
     for (auto &r : active) {
       nets.push_back(r->net);
-      steps.push_back(std::min(r->remaining, s->quantum));
+      int64_t st = s->quantum;
+      if (r->step_ms > 0.0 && target_ms > 0.0) {
+        const int64_t cap = r->req.record_raster ? s->quantum : kRoundMaxSteps;
+        st = std::max<int64_t>(1, std::min<int64_t>(cap, (int64_t)(target_ms / r->step_ms)));
+      }
+      steps.push_back((int32_t)std::min<int64_t>(r->remaining, st));
     }
     double ms = 0.0;
     int64_t nl = 0;
@@ -178,6 +201,7 @@ static void round_loop(g4s_server *s) {
       if (rc != 0) r->status = rc;
       g4s_net_info inf{};
       if (rc == 0 && g4s_net_get_info(r->net, &inf) == 0) ev += inf.last_run_spikes * (int64_t)r->req.nsyn;
+      if (rc == 0 && steps[i] > 0) r->step_ms = net_recent_step_ms(r->net, steps[i]);
       r->remaining -= steps[i];
       if (r->remaining <= 0 || rc != 0) {
         finish_request(s, r);

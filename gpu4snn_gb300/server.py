@@ -24,8 +24,10 @@ class Result:
 
 
 class Server:
-    """Requests are admitted while they fit `hbm_budget_bytes` and advanced together by up
-    to `quantum` steps per persistent launch; arrivals join at the next round."""
+    """Requests are admitted while they fit `hbm_budget_bytes` and advanced together, one
+    persistent launch per round: `quantum` steps in a request's first round, then as many as
+    the median resident request runs in `quantum` steps (rounds of even duration); arrivals
+    join at the next round."""
 
     def __init__(self, hbm_budget_bytes: int, quantum: int = 250):
         h = C.c_void_p()

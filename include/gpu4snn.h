@@ -191,8 +191,11 @@ int g4s_run_protocol(int32_t n, int32_t nsyn, int32_t iterations, int32_t algori
 /* Serving with continuous batching (no counterpart in the reference, which runs one
  * experiment per process, gpu4snn.py:42).  A server admits submitted simulations while
  * their estimated device bytes fit `hbm_budget_bytes`, keeps them resident, and advances
- * all resident ones together by up to `quantum_steps` steps per persistent launch of the
- * SKL team kernel; requests arriving meanwhile join at the next round.  submit/poll/
+ * all resident ones together in one persistent launch of the SKL team kernel per round:
+ * `quantum_steps` steps in a request's first round, then as many as the median resident
+ * request runs in `quantum_steps` steps, from the measured per-step times (at most
+ * `quantum_steps` for a request that records its raster); requests arriving meanwhile
+ * join at the next round.  submit/poll/
  * result/release/get_stats are thread-safe. */
 typedef struct g4s_request {
   int64_t n;           /* neurons                                   */
