@@ -23,6 +23,7 @@
 #include <tuple>
 #include <new>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/gpu4snn.h"
@@ -62,6 +63,7 @@ struct TeamLaunch {
   // the round as a CUDA graph, replayed while its shape (networks, teams, buffers) holds
   cudaGraphExec_t exec = nullptr;
   std::vector<uint64_t> sig;
+  std::vector<int> order;  // networks of the round in flight (team_round_start .. finish)
   void drop_graph() {
     if (exec) cudaGraphExecDestroy(exec);
     exec = nullptr;
@@ -623,33 +625,64 @@ static int chunk_copy_raster(g4s_net *n, int cs, cudaStream_t s) {
   return G4S_OK;
 }
 
-static void chunk_finish(g4s_net *n, int cs, int64_t *spikes) {
-  const int64_t total = chunk_total(n, cs);
+// One step's ids in ascending order.  The team kernel writes them rank by rank (ranks own
+// ascending ranges), each rank's few ids in arrival order, so an insertion sort finishes in
+// a few shifts per id; an order far from sorted (a one-CTA team's ids) goes to std::sort
+// once the shifts exceed a small multiple of the count.
+static void sort_step_ids(int *b, int cnt) {
+  int64_t budget = 4 * (int64_t)cnt + 64;
+  for (int i = 1; i < cnt; ++i) {
+    const int x = b[i];
+    int j = i;
+    while (j > 0 && b[j - 1] > x) {
+      b[j] = b[j - 1];
+      --j;
+      if (--budget < 0) {
+        b[j] = x;
+        std::sort(b, b + cnt);
+        return;
+      }
+    }
+    b[j] = x;
+  }
+}
+
+// The host side of a finished chunk that began at step t0, from its per-step counts, raster
+// offsets and stamps and the raster in the pinned staging buffer: the sorted raster (kept
+// or streamed to its file), the counts and the per-step times.
+static void chunk_finish_from(g4s_net *n, int cs, const int *counts, const long long *base,
+                              const unsigned long long *stamps, int64_t t0, int64_t *spikes) {
+  const int64_t total = (int64_t)base[cs - 1] + counts[cs - 1];
   if (n->desc.record_raster && n->rstream) {
-    for (int lt = 0; lt < cs; ++lt) std::sort(n->h_raster + n->h_base[lt], n->h_raster + n->h_base[lt] + n->h_counts[lt]);
-    raster_push(n->rstream, n->h_counts, cs, n->h_raster, total);
+    for (int lt = 0; lt < cs; ++lt) sort_step_ids(n->h_raster + base[lt], counts[lt]);
+    raster_push(n->rstream, counts, cs, n->h_raster, total);
   } else if (n->desc.record_raster && total > 0) {
     const size_t off = n->rt.size();
     n->rt.resize(off + (size_t)total);
     n->rid.resize(off + (size_t)total);
     for (int lt = 0; lt < cs; ++lt) {
-      int *b = n->h_raster + n->h_base[lt];
-      std::sort(b, b + n->h_counts[lt]);
-      const int32_t t = (int32_t)(n->t_abs + lt);
-      for (int q = 0; q < n->h_counts[lt]; ++q) {
-        n->rt[off + (size_t)n->h_base[lt] + q] = t;
-        n->rid[off + (size_t)n->h_base[lt] + q] = b[q];
+      int *b = n->h_raster + base[lt];
+      sort_step_ids(b, counts[lt]);
+      const int32_t t = (int32_t)(t0 + lt);
+      int32_t *rt = n->rt.data() + off + (size_t)base[lt], *rid = n->rid.data() + off + (size_t)base[lt];
+      for (int q = 0; q < counts[lt]; ++q) {
+        rt[q] = t;
+        rid[q] = b[q];
       }
     }
   }
   for (int lt = 0; lt < cs; ++lt) {
-    n->counts.push_back(n->h_counts[lt]);
-    const unsigned long long s0 = n->h_stamps[2 * lt], s1 = n->h_stamps[2 * lt + 1];
-    const unsigned long long s2 = lt + 1 < cs ? n->h_stamps[2 * lt + 2] : 0ull;
+    n->counts.push_back(counts[lt]);
+    const unsigned long long s0 = stamps[2 * lt], s1 = stamps[2 * lt + 1];
+    const unsigned long long s2 = lt + 1 < cs ? stamps[2 * lt + 2] : 0ull;
     n->upd_ms.push_back(s1 > s0 ? (float)((s1 - s0) * 1e-6) : 0.0f);
     n->step_ms.push_back(s2 > s0 ? (float)((s2 - s0) * 1e-6) : 0.0f);
   }
   *spikes = total;
+}
+
+static void chunk_finish(g4s_net *n, int cs, int64_t *spikes) {
+  chunk_finish_from(n, cs, n->h_counts, n->h_base, n->h_stamps, n->t_abs, spikes);
   n->t_abs += cs;
 }
 
@@ -666,23 +699,20 @@ static int absorb_chunk(g4s_net *n, int cs, int64_t *spikes) {
   return G4S_OK;
 }
 
-// The same after a team round, whose graph copied the counts, offsets and stamps.
-static int absorb_raster(g4s_net *n, int cs, int64_t *spikes) {
-  int rc = chunk_copy_raster(n, cs, n->stream);
-  if (rc) return rc;
-  G4S_CUDA(cudaStreamSynchronize(n->stream));
-  chunk_finish(n, cs, spikes);
-  return G4S_OK;
-}
 
 // ---------------------------------------------------------------------------------------
 // One launch of the team kernel over several networks (a "round"): network i advances
 // steps[i] steps (at most its chunk length).  Multi-CTA teams are queued first, then the
 // one-CTA teams by decreasing work, so that long networks start early.
 // ---------------------------------------------------------------------------------------
-static int team_round(g4s_net *const *nets, const int *steps, const bool *last, int count, TeamLaunch &L,
-                      cudaStream_t s, unsigned long long limit_ns, int stall, double *kernel_ms, int64_t *launches) {
+// team_round_start enqueues the round on stream s and returns; team_round_finish waits for
+// it and checks every network's status words.  Between the two, the host may work on the
+// previous round's results, but must not touch the pinned per-step buffers (the round's
+// graph writes them at its end) nor the networks' device arrays.
+static int team_round_start(g4s_net *const *nets, const int *steps, const bool *last, int count, TeamLaunch &L,
+                            cudaStream_t s, unsigned long long limit_ns, int stall) {
   std::vector<int> order;
+  L.order.clear();
   int nslots = 0, maxteam = 1;
   size_t smem = 16;
   for (int i = 0; i < count; ++i)
@@ -796,16 +826,28 @@ static int team_round(g4s_net *const *nets, const int *steps, const bool *last, 
     L.sig = sig;
   }
   G4S_CUDA(cudaGraphLaunch(L.exec, s));
+  L.order = order;
+  return G4S_OK;
+}
+
+static int team_round_finish(TeamLaunch &L, cudaStream_t s, double *kernel_ms, int64_t *launches) {
+  if (L.order.empty()) return G4S_OK;  // nothing was launched
   G4S_CUDA(cudaStreamSynchronize(s));
   float ms = 0.0f;
   G4S_CUDA(cudaEventElapsedTime(&ms, L.e0, L.e1));
   *kernel_ms += ms;
   *launches += 1;
-  for (int i : order) {
-    rc = status_rc(L.h_status[2 * i], L.h_status[2 * i + 1], "team step kernel");
+  for (int i : L.order) {
+    const int rc = status_rc(L.h_status[2 * i], L.h_status[2 * i + 1], "team step kernel");
     if (rc) return rc;
   }
   return G4S_OK;
+}
+
+static int team_round(g4s_net *const *nets, const int *steps, const bool *last, int count, TeamLaunch &L,
+                      cudaStream_t s, unsigned long long limit_ns, int stall, double *kernel_ms, int64_t *launches) {
+  const int rc = team_round_start(nets, steps, last, count, L, s, limit_ns, stall);
+  return rc ? rc : team_round_finish(L, s, kernel_ms, launches);
 }
 
 static int run_net(g4s_net *n, int32_t steps, int32_t alg_in) {
@@ -824,16 +866,48 @@ static int run_net(g4s_net *n, int32_t steps, int32_t alg_in) {
   G4S_CUDA(cudaEventRecord(n->ev0, n->stream));
   int64_t remaining = steps, spikes = 0, launches = 0;
   double kernel_ms = 0.0;
-  while (remaining > 0) {
-    const int cs = (int)std::min<int64_t>(remaining, team ? n->chunk_steps : n->chunk_legacy);
-    const bool last_chunk = remaining == cs;
-    if (team) {
+  if (team) {
+    // Chunks as team rounds, pipelined: once a round has ended and its raster is copied
+    // down, the next round is launched, and the host sorts and files the finished chunk
+    // while the GPU runs the next one.
+    std::vector<int> mc;
+    std::vector<long long> mb;
+    std::vector<unsigned long long> ms;
+    int cs = 0;
+    auto start = [&]() -> int {
+      cs = (int)std::min<int64_t>(remaining, n->chunk_steps);
+      const bool last_chunk = remaining == cs;
       g4s_net *one[1] = {n};
-      int rc = team_round(one, &cs, &last_chunk, 1, n->launch, n->stream, n->barrier_ns, n->barrier_stall,
-                          &kernel_ms, &launches);
+      const int rc = team_round_start(one, &cs, &last_chunk, 1, n->launch, n->stream, n->barrier_ns, n->barrier_stall);
       n->barrier_stall = 0;
-      if (rc) return rc;
-    } else {
+      remaining -= cs;
+      return rc;
+    };
+    int rc = remaining > 0 ? start() : G4S_OK;
+    if (rc) return rc;
+    while (cs > 0) {
+      if ((rc = team_round_finish(n->launch, n->stream, &kernel_ms, &launches))) return rc;
+      // this chunk's per-step arrays, out of the pinned buffers the next round's graph
+      // writes, and its raster, out of the device buffer the next round overwrites
+      mc.assign(n->h_counts, n->h_counts + cs);
+      mb.assign(n->h_base, n->h_base + cs);
+      ms.assign(n->h_stamps, n->h_stamps + 2 * (size_t)cs);
+      if ((rc = chunk_copy_raster(n, cs, n->stream))) return rc;
+      G4S_CUDA(cudaStreamSynchronize(n->stream));
+      const int done = cs;
+      const int64_t t0 = n->t_abs;
+      n->t_abs += done;
+      cs = 0;
+      if (remaining > 0 && (rc = start())) return rc;
+      int64_t chunk_spikes = 0;
+      chunk_finish_from(n, done, mc.data(), mb.data(), ms.data(), t0, &chunk_spikes);
+      spikes += chunk_spikes;
+    }
+  }
+  while (!team && remaining > 0) {
+    const int cs = (int)std::min<int64_t>(remaining, n->chunk_legacy);
+    const bool last_chunk = remaining == cs;
+    {
       G4S_CUDA(cudaMemsetAsync(v.counts, 0, (size_t)cs * sizeof(int), n->stream));
       G4S_CUDA(cudaMemsetAsync(v.stamps, 0, ((size_t)cs * 2 + 2) * 8, n->stream));
       if (alg == kAlgSKL) G4S_CUDA(cudaMemsetAsync(n->gs, 0, sizeof(GridSync), n->stream));
@@ -858,8 +932,7 @@ static int run_net(g4s_net *n, int32_t steps, int32_t alg_in) {
       kernel_ms += kms;
     }
     int64_t chunk_spikes = 0;
-    // (a team round's graph already copied the per-step counts, offsets and stamps back)
-    int rc = team ? absorb_raster(n, cs, &chunk_spikes) : absorb_chunk(n, cs, &chunk_spikes);
+    int rc = absorb_chunk(n, cs, &chunk_spikes);
     if (rc) return rc;
     spikes += chunk_spikes;
     remaining -= cs;
@@ -1188,11 +1261,29 @@ int g4s_net_load_tables(g4s_net *n, const int32_t *idx, const float *w, int32_t 
   if (stride != v.stride)
     return set_error(G4S_ERR_INVALID, "table stride must be " + std::to_string(v.stride));
   const size_t cnt = (size_t)v.n * (size_t)v.stride, bytes = cnt * 4;
-  // every target must be a neuron of this network or negative (an unused slot)
-  for (size_t k = 0; k < cnt; ++k)
-    if (idx[k] >= v.n)
-      return set_error(G4S_ERR_INVALID, "table entry " + std::to_string(k) + " targets neuron " +
-                                            std::to_string(idx[k]) + " >= n");
+  // every target must be a neuron of this network or negative (an unused slot): checked on
+  // all host cores, the first offending entry reported
+  {
+    const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    const size_t parts = cnt >= ((size_t)1 << 22) ? hw : 1, per = (cnt + parts - 1) / parts;
+    std::vector<size_t> bad(parts, SIZE_MAX);
+    auto scan = [&](size_t p) {
+      const size_t end = std::min(cnt, (p + 1) * per);
+      for (size_t k = p * per; k < end; ++k)
+        if (idx[k] >= v.n) {
+          bad[p] = k;
+          return;
+        }
+    };
+    std::vector<std::thread> pool;
+    for (size_t p = 1; p < parts; ++p) pool.emplace_back(scan, p);
+    scan(0);
+    for (auto &t : pool) t.join();
+    for (size_t k : bad)
+      if (k != SIZE_MAX)
+        return set_error(G4S_ERR_INVALID, "table entry " + std::to_string(k) + " targets neuron " +
+                                              std::to_string(idx[k]) + " >= n");
+  }
   G4S_CUDA(cudaMemcpyAsync(const_cast<int *>(v.idx), idx, bytes, cudaMemcpyHostToDevice, n->stream));
   G4S_CUDA(cudaMemcpyAsync(const_cast<float *>(v.w), w, bytes, cudaMemcpyHostToDevice, n->stream));
   return finish_tables(n);
