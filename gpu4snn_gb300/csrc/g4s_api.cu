@@ -581,7 +581,15 @@ static int prepare_team(g4s_net *n, bool batch = false) {
 // of the split shared-memory accumulation is measured here: fewer than 65536 synapses
 // into any neuron and sum(|q| >> 16) + 1 over them below 2^31 - 2^20.
 static int finish_tables(g4s_net *n) {
-  G4S_CUDA(launch_sort_rows(n->v, n->stream));
+  // (rows that arrive sorted, as tables read back from a network do, skip the sort)
+  int *flag = nullptr, h_unsorted = 1;
+  cudaError_t ef = cudaMalloc((void **)&flag, sizeof(int));
+  if (ef == cudaSuccess) ef = launch_rows_sorted(n->v, flag, n->stream);
+  if (ef == cudaSuccess) ef = cudaMemcpyAsync(&h_unsorted, flag, sizeof(int), cudaMemcpyDeviceToHost, n->stream);
+  if (ef == cudaSuccess) ef = cudaStreamSynchronize(n->stream);
+  cudaFree(flag);
+  if (ef != cudaSuccess) return cuda_error(ef, "row order check");
+  if (h_unsorted) G4S_CUDA(launch_sort_rows(n->v, n->stream));
   n->team_ready = false;
   n->pair_ready = false;
   unsigned *cnt = nullptr;

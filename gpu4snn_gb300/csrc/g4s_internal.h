@@ -127,6 +127,8 @@ inline int team_window(int64_t rc, int team) {
   return (int)(cap > (size_t)kMaxWindow ? kMaxWindow : cap & ~(size_t)7);
 }
 cudaError_t launch_sort_rows(const NetView &v, cudaStream_t s);
+// *unsorted <- 1 if some row is not in launch_sort_rows' order, else 0
+cudaError_t launch_rows_sorted(const NetView &v, int *unsorted, cudaStream_t s);
 cudaError_t launch_segoff(const NetView &v, int team, int64_t rc, uint16_t *seg, cudaStream_t s);
 cudaError_t launch_inbound(const NetView &v, unsigned *cnt, unsigned long long *mag, unsigned long long *out,
                            cudaStream_t s);

@@ -105,6 +105,18 @@ __global__ void k_sort_rows(NetView v, int p2) {
   }
 }
 
+// Rows already in the sort's order (ascending 64-bit keys target << 32 | weight bits, the
+// targets taken as unsigned so that unused slots come last)?  *unsorted = 1 if not.
+__global__ void k_rows_sorted(NetView v, int *unsorted) {
+  const int64_t total = v.n * (int64_t)v.stride;
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < total; g += (int64_t)gridDim.x * blockDim.x) {
+    if ((g + 1) % v.stride == 0) continue;  // the last slot of a row
+    const unsigned long long a = ((unsigned long long)(unsigned)v.idx[g] << 32) | __float_as_uint(v.w[g]);
+    const unsigned long long b = ((unsigned long long)(unsigned)v.idx[g + 1] << 32) | __float_as_uint(v.w[g + 1]);
+    if (a > b) *unsorted = 1;
+  }
+}
+
 // Segment table: seg[row][k] = first slot of the sorted row whose target is >= k*Rc, for
 // k = 0..T (unused slots compare as huge and lie beyond seg[row][T]).  One warp per row,
 // one binary search per boundary.
@@ -835,6 +847,16 @@ cudaError_t launch_team(const TeamItem *items, const int2 *slots, const int *nsl
   cfg.numAttrs = 1;
   return pair ? cudaLaunchKernelEx(&cfg, k_team<kTeamNT, true>, items, slots, nslots, slot_head, limit_ns, stall)
               : cudaLaunchKernelEx(&cfg, k_team<kTeamNT, false>, items, slots, nslots, slot_head, limit_ns, stall);
+}
+
+cudaError_t launch_rows_sorted(const NetView &v, int *unsorted, cudaStream_t s) {
+  int dev = 0, sms = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaError_t e = cudaMemsetAsync(unsorted, 0, sizeof(int), s);
+  if (e != cudaSuccess) return e;
+  k_rows_sorted<<<(unsigned)(sms * 8), 512, 0, s>>>(v, unsorted);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_sort_rows(const NetView &v, cudaStream_t s) {

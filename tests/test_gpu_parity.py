@@ -189,6 +189,27 @@ def test_uploaded_tables_with_holes(g4s, oracle):
             compare_state(net, sim)
 
 
+def test_sorted_and_shuffled_uploads_agree(g4s):
+    """Rows uploaded in the device's sorted order skip the row sort; the same rows shuffled
+    are sorted first.  Both give the same device tables and the same run."""
+    n, nsyn, seed = 20_000, 500, 14
+    with g4s.Network(n, nsyn, seed=seed) as ref:
+        idx, w = ref.tables()
+        ref.run(200, 4)
+        t_ref, i_ref = ref.raster()
+    rng = np.random.default_rng(3)
+    perm = np.argsort(rng.random(idx.shape), axis=1)
+    shuffled = (np.take_along_axis(idx, perm, axis=1), np.take_along_axis(w, perm, axis=1))
+    assert not np.array_equal(shuffled[0], idx)
+    for tabs in ((idx, w), shuffled):
+        with g4s.Network(n, nsyn, seed=seed, tables=tabs) as net:
+            gi, gw = net.tables()
+            assert np.array_equal(gi, idx) and np.array_equal(gw.view(np.uint32), w.view(np.uint32))
+            net.run(200, 4)
+            t, i = net.raster()
+            assert np.array_equal(t, t_ref) and np.array_equal(i, i_ref)
+
+
 @pytest.mark.parametrize("p", [0, 8])
 def test_weights_of_every_magnitude(g4s, oracle, p):
     """Weights spread over 2^-34 .. 2^4 (tiny ones round in Q32.32, ties included), both
