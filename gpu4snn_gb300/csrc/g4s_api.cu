@@ -906,10 +906,11 @@ static int run_net(g4s_net *n, int32_t steps, int32_t alg_in) {
       const int64_t t0 = n->t_abs;
       n->t_abs += done;
       cs = 0;
-      if (remaining > 0 && (rc = start())) return rc;
-      int64_t chunk_spikes = 0;
+      const int rs = remaining > 0 ? start() : G4S_OK;
+      int64_t chunk_spikes = 0;  // (the finished chunk is filed even if the next launch failed)
       chunk_finish_from(n, done, mc.data(), mb.data(), ms.data(), t0, &chunk_spikes);
       spikes += chunk_spikes;
+      if (rs) return rs;
     }
   }
   while (!team && remaining > 0) {
