@@ -365,6 +365,8 @@ def main():
     if alg == g.ALG_AUTO:
         talg, tteam, tus = net.autotune(min(T, 200))
         tuned = {"algorithm": talg, "name": ALG_LABEL[talg], "team": tteam, "us_per_step": tus}
+        net.run(8, alg)  # (applies the choice, so that its CTA size can be read back)
+        tuned["block_threads"] = net.block_threads()
     for _ in range(a.warmup):
         net.run(T, alg)
     runs = []
@@ -401,7 +403,7 @@ def main():
     upd_ms = sum(r[4] for r in runs)
     deliv_ms = max(1e-9, sum(r[5] for r in runs) - upd_ms)
     if last_alg == g.ALG_SKL and team > 0:
-        kname = f"k_team (SKL team kernel: {team} CTAs x 1024 threads, {slice_} neurons per CTA)"
+        kname = f"k_team (SKL team kernel: {team} CTAs x {net.block_threads()} threads, {slice_} neurons per CTA)"
     elif last_alg == g.ALG_SKL:
         kname = "k_persistent (SKL global-atomic kernel)"
     else:

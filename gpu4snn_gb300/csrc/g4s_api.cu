@@ -119,6 +119,7 @@ struct TuneChoice {
   int alg = kAlgSKL;
   int team = 0;
   int mode = kDeliverRun;
+  int nt = kTeamNT;  // threads per CTA of the team kernel
 };
 
 // ---------------------------------------------------------------------------------------
@@ -168,6 +169,7 @@ struct g4s_net {
   size_t seg_bytes = 0;
   int want_p = 0;
   int deliver_mode = kDeliverRun;
+  int team_nt = kTeamNT;  // threads per CTA of its team rounds (kTeamNT or kTeamNTSmall)
   bool tables_fit = false;
   unsigned long long max_in = 0, max_mag = 0;
   TeamLaunch launch;
@@ -478,7 +480,10 @@ static int resolve_alg(g4s_net *n, int alg) {
     n->team_ready = false;
     n->team_ok = true;
   }
-  if (c.alg == kAlgSKL) n->deliver_mode = c.mode;
+  if (c.alg == kAlgSKL) {
+    n->deliver_mode = c.mode;
+    n->team_nt = c.nt;
+  }
   return c.alg;
 }
 
@@ -493,7 +498,7 @@ static bool plan_team(g4s_net *n, int want, bool batch, int *p_out, int64_t *rc_
   const NetView &v = n->v;
   if (!n->tables_fit) return false;
   int pmax = 0;
-  if (team_max_blocks(kTeamSmemLimit, &pmax) != cudaSuccess || pmax < 1) {
+  if (team_max_blocks(kTeamSmemLimit, &pmax, n->team_nt) != cudaSuccess || pmax < 1) {
     (void)cudaGetLastError();
     return false;
   }
@@ -510,7 +515,7 @@ static bool plan_team(g4s_net *n, int want, bool batch, int *p_out, int64_t *rc_
     if (team_smem(rc, (int)p) == 0) return false;
   }
   int pfit = 0;
-  if (team_max_blocks(team_smem(rc, (int)p), &pfit) != cudaSuccess || pfit < p) {
+  if (team_max_blocks(team_smem(rc, (int)p), &pfit, n->team_nt) != cudaSuccess || pfit < p) {
     (void)cudaGetLastError();
     return false;
   }
@@ -741,8 +746,11 @@ static int team_round_start(g4s_net *const *nets, const int *steps, const bool *
   if (rc) return rc;
   bool pair = true;  // every network of the round has its interleaved rows
   for (int i : order) pair = pair && nets[i]->v.pair != nullptr;
+  int nt = nets[order[0]]->team_nt;  // threads per CTA: the networks' own when they agree
+  for (int i : order)
+    if (nets[i]->team_nt != nt) nt = kTeamNT;
   int gmax = 0;
-  G4S_CUDA(team_max_blocks(smem, &gmax));  // also raises the kernel's shared-memory ceiling
+  G4S_CUDA(team_max_blocks(smem, &gmax, nt));  // also raises the kernel's shared-memory ceiling
   if (gmax < maxteam) return set_error(G4S_ERR_CUDA, "team larger than the co-resident grid");
   const int grid = std::min(nslots, gmax);
   // this round's descriptors, in pinned host memory the graph copies from
@@ -784,7 +792,7 @@ static int team_round_start(g4s_net *const *nets, const int *steps, const bool *
   // graph, so the key holds each network's creation number as well as its addresses.
   auto u = [](const void *p) { return (uint64_t)(uintptr_t)p; };
   std::vector<uint64_t> sig = {(uint64_t)count, (uint64_t)nslots, (uint64_t)grid, (uint64_t)smem, limit_ns,
-                               (uint64_t)stall, (uint64_t)pair, u(L.d_items), u(L.d_slots), u(L.d_ctl), u(L.h_items),
+                               (uint64_t)stall, (uint64_t)pair, (uint64_t)nt, u(L.d_items), u(L.d_slots), u(L.d_ctl), u(L.h_items),
                                u(L.h_slots), u(L.h_ctl), u(L.h_status), u(L.e0), u(L.e1)};
   for (int i : order) {
     const g4s_net *n = nets[i];
@@ -810,7 +818,7 @@ static int team_round_start(g4s_net *const *nets, const int *steps, const bool *
     if (e == cudaSuccess) e = cudaMemcpyAsync(L.d_ctl, L.h_ctl, 8, cudaMemcpyHostToDevice, s);
     // (external records: the graph records the events at every replay)
     if (e == cudaSuccess) e = cudaEventRecordWithFlags(L.e0, s, cudaEventRecordExternal);
-    if (e == cudaSuccess) e = launch_team(L.d_items, L.d_slots, L.d_ctl, L.d_ctl + 1, grid, smem, limit_ns, stall, s, pair);
+    if (e == cudaSuccess) e = launch_team(L.d_items, L.d_slots, L.d_ctl, L.d_ctl + 1, grid, smem, limit_ns, stall, s, pair, nt);
     if (e == cudaSuccess) e = cudaEventRecordWithFlags(L.e1, s, cudaEventRecordExternal);
     for (int i : order) {
       const g4s_net *n = nets[i];
@@ -1093,16 +1101,19 @@ static int autotune(g4s_net *n, int32_t probe, TuneChoice *best, double *best_us
   if (pmax > 1) teams.push_back(pmax);
   // segment-run delivery only: lane-per-spike measured slower or equal on every
   // configuration tried (it stays available through g4s_net_set_geometry)
-  for (int p : teams) cand.push_back(TuneChoice{kAlgSKL, p, kDeliverRun});
+  // each team size with both CTA sizes of the team kernel
+  for (int p : teams)
+    for (int nt : {kTeamNT, kTeamNTSmall}) cand.push_back(TuneChoice{kAlgSKL, p, kDeliverRun, nt});
   cand.push_back(TuneChoice{kAlgAB, 0, kDeliverRun});
   cand.push_back(TuneChoice{kAlgAP, 0, kDeliverRun});
-  const int keep_mode = n->deliver_mode;
+  const int keep_mode = n->deliver_mode, keep_nt = n->team_nt;
   double best_t = 1e300, rate = 0.0;
   TuneChoice pick = cand[0];
   for (const TuneChoice &c : cand) {
     if (c.alg == kAlgSKL) {
       n->want_p = c.team;
       n->deliver_mode = c.mode;
+      n->team_nt = c.nt;
       n->team_ready = false;
       n->team_ok = true;
       if ((rc = prepare_team(n))) break;
@@ -1121,6 +1132,7 @@ static int autotune(g4s_net *n, int32_t probe, TuneChoice *best, double *best_us
   }
   n->want_p = keep_p;
   n->deliver_mode = keep_mode;
+  n->team_nt = keep_nt;
   n->team_ready = false;
   n->team_ok = true;
   if (rc) return rc;
@@ -1307,6 +1319,22 @@ int g4s_net_set_geometry(g4s_net *n, int32_t owner_blocks, int32_t delivery) {
   n->deliver_mode = delivery;
   n->team_ready = false;
   n->team_ok = true;
+  return G4S_OK;
+}
+
+int g4s_net_set_block_threads(g4s_net *n, int32_t threads) {
+  if (!n) return set_error(G4S_ERR_INVALID, "null handle");
+  if (threads != kTeamNT && threads != kTeamNTSmall)
+    return set_error(G4S_ERR_INVALID, "threads must be 1024 or 768");
+  n->team_nt = threads;
+  n->team_ready = false;
+  n->team_ok = true;
+  return G4S_OK;
+}
+
+int g4s_net_get_block_threads(g4s_net *n, int32_t *threads) {
+  if (!n || !threads) return set_error(G4S_ERR_INVALID, "null argument");
+  *threads = n->team_nt;
   return G4S_OK;
 }
 

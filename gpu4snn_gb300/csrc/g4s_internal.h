@@ -134,12 +134,18 @@ cudaError_t launch_inbound(const NetView &v, unsigned *cnt, unsigned long long *
                            cudaStream_t s);
 // team_max_blocks also raises the kernel's shared-memory ceiling: call it once before the
 // first launch_team (which may then be captured in a CUDA graph)
-// pair: the tables are read from v.pair (interleaved rows) instead of v.idx and v.w
+// Threads per CTA of the team kernel: 1024 (the default; the most reads in flight) or 768
+// (80 registers a thread instead of 64: no spills, faster when a step's work is small).
+constexpr int kTeamNT = 1024;
+constexpr int kTeamNTSmall = 768;
+// pair: the tables are read from v.pair (interleaved rows) instead of v.idx and v.w;
+// nt: kTeamNT or kTeamNTSmall threads per CTA
 cudaError_t launch_team(const TeamItem *items, const int2 *slots, const int *nslots, int *slot_head, int grid,
-                        size_t smem, unsigned long long limit_ns, int stall, cudaStream_t s, bool pair);
+                        size_t smem, unsigned long long limit_ns, int stall, cudaStream_t s, bool pair,
+                        int nt = kTeamNT);
 // v.pair <- the rows of v.idx and v.w interleaved (after every change of the tables)
 cudaError_t launch_pairs(const NetView &v, cudaStream_t s);
-cudaError_t team_max_blocks(size_t smem, int *out);
+cudaError_t team_max_blocks(size_t smem, int *out, int nt = kTeamNT);
 // mean duration in ms of the last k simulated steps of a handle with a step time (0: none)
 double net_recent_step_ms(const g4s_net *n, int64_t k);
 cudaError_t team_smem_ceiling();  // the part of team_max_blocks that launch_team needs

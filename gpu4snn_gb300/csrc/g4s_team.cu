@@ -209,10 +209,11 @@ struct TeamShared {
 };
 
 // Record words of a rank per step: word 0 = spike count, words 1.. = ids (kInline inline);
-// a thread reads up to kSlots 16-byte slots of a step's records.
+// a thread of an NT-thread CTA reads up to slots_per_thread(NT) 16-byte slots of a step's
+// records.
 constexpr int kRankWords = kRecLines * kRecWords;
 constexpr int kInline = kRankWords - 1;
-constexpr int kSlots = (kMaxTeam * kRankWords / 2 + 1023) / 1024;
+__host__ __device__ constexpr int slots_per_thread(int nt) { return (kMaxTeam * kRankWords / 2 + nt - 1) / nt; }
 constexpr int kLine1After = 7;
 constexpr int kFlatMinSpikes = 128;  // fewer spikes: run delivery (the flat one's scan costs more)  // line 1 of a rank is read if it had more spikes in the previous step
 
@@ -271,6 +272,7 @@ __device__ void team_run(const TeamItem &it, int rank, unsigned char *s_raw, Tea
   const unsigned segw = (unsigned)T + 1;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   constexpr int kWarps = NT / 32;
+  constexpr int kSlots = slots_per_thread(NT);
   const bool solo = T == 1;   // the whole network in this CTA: no exchange
   const bool lead = rank == 0 && threadIdx.x == 0;
   // synapse `off` of the tables: one 8-byte load from the interleaved rows, or two loads
@@ -515,9 +517,9 @@ __device__ void team_run(const TeamItem &it, int rank, unsigned char *s_raw, Tea
         __syncthreads();
         if (sh.fail) return;
       }
-      if (!solo && !gl && K >= kFlatMinSpikes && L.flat) {
+      if (!solo && !gl && K >= kFlatMinSpikes && L.flat && K <= 4 * NT) {
         // segment bounds and their offsets in the concatenation (for the flat delivery):
-        // thread t takes spikes 4t .. 4t+3 (K <= cap <= 4 NT); a block scan of their
+        // thread t takes spikes 4t .. 4t+3 (K <= 4 NT); a block scan of their
         // lengths (every warp scans the warp sums itself), then each thread marks the
         // synapses of its spikes with the spike's index
         const uint64_t pkeep = policy_evict_last();
@@ -542,7 +544,7 @@ __device__ void team_run(const TeamItem &it, int rank, unsigned char *s_raw, Tea
         }
         if (lane == 31) s_wsum[warp] = incl;
         __syncthreads();
-        const int ws = s_wsum[lane];
+        const int ws = lane < kWarps ? s_wsum[lane] : 0;
         int wi = ws;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -794,7 +796,6 @@ __global__ void __launch_bounds__(NT, 1) k_team(const TeamItem *__restrict__ ite
 // ---------------------------------------------------------------------------------------
 // Launchers.
 // ---------------------------------------------------------------------------------------
-constexpr int kTeamNT = 1024;
 
 size_t team_smem(int64_t rc, int team) {
   if (rc < 1 || team < 1 || team > kMaxTeam) return 0;
@@ -807,23 +808,36 @@ size_t team_smem(int64_t rc, int team) {
 // The kernel's shared-memory ceiling is always the largest layout's (every team layout
 // stays under it), so host threads that launch teams of different sizes never lower it
 // under one another, and a captured launch needs no attribute call.
-cudaError_t team_smem_ceiling() {
-  cudaError_t e = cudaFuncSetAttribute(k_team<kTeamNT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)kTeamSmemLimit);
+template <int NT>
+static cudaError_t team_ceiling_nt() {
+  cudaError_t e = cudaFuncSetAttribute(k_team<NT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTeamSmemLimit);
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(k_team<kTeamNT, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTeamSmemLimit);
+    e = cudaFuncSetAttribute(k_team<NT, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTeamSmemLimit);
   return e;
 }
 
-cudaError_t team_max_blocks(size_t smem, int *out) {
-  if (smem > kTeamSmemLimit) return cudaErrorInvalidValue;
+cudaError_t team_smem_ceiling() {
+  cudaError_t e = team_ceiling_nt<kTeamNT>();
+  return e == cudaSuccess ? team_ceiling_nt<kTeamNTSmall>() : e;
+}
+
+// CTAs of the team kernel with `smem` bytes of shared memory that fit an SM (both table
+// layouts' instantiations; they need the same resources)
+template <int NT>
+static cudaError_t team_occupancy(size_t smem, int *occ) {
+  int a = 0, b = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_team<NT, true>, NT, smem);
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_team<NT, false>, NT, smem);
+  *occ = a < b ? a : b;
+  return e;
+}
+
+cudaError_t team_max_blocks(size_t smem, int *out, int nt) {
+  if (smem > kTeamSmemLimit || (nt != kTeamNT && nt != kTeamNTSmall)) return cudaErrorInvalidValue;
   cudaError_t e = team_smem_ceiling();
   if (e != cudaSuccess) return e;
   int occ = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_team<kTeamNT, true>, kTeamNT, smem);
-  int occ2 = 0;  // both layouts' instantiations (the same resources)
-  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ2, k_team<kTeamNT, false>, kTeamNT, smem);
-  occ = occ2 < occ ? occ2 : occ;
+  e = nt == kTeamNT ? team_occupancy<kTeamNT>(smem, &occ) : team_occupancy<kTeamNTSmall>(smem, &occ);
   if (e != cudaSuccess) return e;
   int dev = 0, sms = 1;
   cudaGetDevice(&dev);
@@ -833,11 +847,11 @@ cudaError_t team_max_blocks(size_t smem, int *out) {
 }
 
 cudaError_t launch_team(const TeamItem *items, const int2 *slots, const int *nslots, int *slot_head, int grid,
-                        size_t smem, unsigned long long limit_ns, int stall, cudaStream_t s, bool pair) {
-  if (smem > kTeamSmemLimit) return cudaErrorInvalidValue;
+                        size_t smem, unsigned long long limit_ns, int stall, cudaStream_t s, bool pair, int nt) {
+  if (smem > kTeamSmemLimit || (nt != kTeamNT && nt != kTeamNTSmall)) return cudaErrorInvalidValue;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)grid);
-  cfg.blockDim = dim3(kTeamNT);
+  cfg.blockDim = dim3((unsigned)nt);
   cfg.dynamicSmemBytes = smem;
   cfg.stream = s;
   cudaLaunchAttribute attr[1];
@@ -845,6 +859,9 @@ cudaError_t launch_team(const TeamItem *items, const int2 *slots, const int *nsl
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
+  if (nt == kTeamNTSmall)
+    return pair ? cudaLaunchKernelEx(&cfg, k_team<kTeamNTSmall, true>, items, slots, nslots, slot_head, limit_ns, stall)
+                : cudaLaunchKernelEx(&cfg, k_team<kTeamNTSmall, false>, items, slots, nslots, slot_head, limit_ns, stall);
   return pair ? cudaLaunchKernelEx(&cfg, k_team<kTeamNT, true>, items, slots, nslots, slot_head, limit_ns, stall)
               : cudaLaunchKernelEx(&cfg, k_team<kTeamNT, false>, items, slots, nslots, slot_head, limit_ns, stall);
 }

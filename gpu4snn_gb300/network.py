@@ -93,6 +93,15 @@ class Network:
         """SKL owner CTAs (0 = automatic) and delivery mapping (0 segment runs, 1 lane per spike)."""
         check(load().g4s_net_set_geometry(self._h, owner_blocks, delivery))
 
+    def set_block_threads(self, threads: int):
+        """Threads per CTA of the SKL team kernel: 1024 (default) or 768 (same results)."""
+        check(load().g4s_net_set_block_threads(self._h, threads))
+
+    def block_threads(self) -> int:
+        t = C.c_int32()
+        check(load().g4s_net_get_block_threads(self._h, C.byref(t)))
+        return t.value
+
     def autotune(self, probe_steps: int = 100) -> tuple[int, int, float]:
         """Time the candidate schemes on this network (state restored afterwards) and keep
         the fastest for ALG_AUTO.  Returns (scheme, team size, us per step)."""

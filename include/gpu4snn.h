@@ -127,6 +127,12 @@ int g4s_net_set_barrier_timeout(g4s_net *net, uint64_t ns);
  * exact-accumulation bound, and the global-atomic persistent kernel runs instead) and the
  * neurons per CTA. */
 int g4s_net_set_geometry(g4s_net *net, int32_t owner_blocks, int32_t delivery);
+/* Threads per CTA of the SKL team kernel: 1024 (the default: the most table reads in
+ * flight, for steps with many synapses per CTA) or 768 (80 registers a thread instead of
+ * 64, no spills: faster for steps whose work is small).  Results do not depend on it; the
+ * autotuner tries both.  A no-alloc run and a batch of networks that disagree use 1024. */
+int g4s_net_set_block_threads(g4s_net *net, int32_t threads);
+int g4s_net_get_block_threads(g4s_net *net, int32_t *threads);
 int g4s_net_get_geometry(g4s_net *net, int32_t *owner_blocks, int64_t *slice);
 
 /* Autotuner (replaces the reference's occupancy-based launch configurator,

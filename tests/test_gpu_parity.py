@@ -169,6 +169,25 @@ def test_owner_geometries(g4s, oracle, p, n, mode):
         compare_state(net, sim)
 
 
+@pytest.mark.parametrize("n,drive,p,mode", [(100_000, 1.0, 0, 0), (50_000, 1.5, 8, 0), (50_000, 1.5, 8, 1),
+                                            (300_000, 1.5, 0, 0), (3000, 1.0, 1, 0)])
+def test_block_threads_768_same_results(g4s, n, drive, p, mode):
+    """The 768-thread team kernel gives the 1024-thread kernel's results bit for bit in every
+    delivery path: the flat mapping (N=100,000), segment runs and one lane per spike on
+    6,250-neuron slices, the dense list of large steps (N=300,000 at drive 1.5), one CTA."""
+    nsyn, out = 1000, []
+    for threads in (1024, 768):
+        with g4s.Network(n, nsyn, seed=17, drive_scale=drive) as net:
+            net.set_geometry(p, mode)
+            net.set_block_threads(threads)
+            assert net.block_threads() == threads
+            net.run(150, 4)
+            out.append((np.stack(net.raster()), net.state()["v"].view(np.uint32).copy(), net.currents()))
+    (ra, va, ca), (rb, vb, cb) = out
+    assert ra.shape[1] > 1000
+    assert np.array_equal(ra, rb) and np.array_equal(va, vb) and np.array_equal(ca, cb)
+
+
 def test_uploaded_tables_with_holes(g4s, oracle):
     """Caller tables may leave slots unused (negative target) anywhere in a row."""
     n, nsyn, seed = 3000, 200, 8
