@@ -44,6 +44,7 @@ WORKLOADS = {
     "n2500": (2500, 1000, 2000, 1.0, 1),
     "n25k": (25_000, 1000, 500, 1.0, 5),  # small profiling case: 0.2 GB of tables, still > L2
     "n300k": (300_000, 1000, 50, 1.0, 6),  # profiling case for large-N delivery: 2.4 GB of tables
+    "n100k_200": (100_000, 1000, 200, 1.0, 2),  # profiling case: the N=100,000 network, 200-step launches
 }
 # algorithmic bytes: delivery = spikes x Nsyn x (4 B target + 4 B weight) and the spike
 # statistics (32 B read + 32 B written per spike); the neuron state (v,u read + write 16 B
@@ -333,6 +334,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="n100k")
     ap.add_argument("--algorithm", default="AUTO")
+    ap.add_argument("--block-threads", type=int, default=0,
+                    help="threads per CTA of the SKL team kernel, 1024 or 768 (0: default / autotuned)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
     ap.add_argument("--raster-budget-mb", type=int, default=0, help="device raster buffer per chunk (0: default)")
@@ -358,6 +361,8 @@ def main():
     alg = g.ALG_NAMES[a.algorithm.upper()] if not a.algorithm.isdigit() else int(a.algorithm)
     budget = a.raster_budget_mb << 20
     net = g.Network(n, nsyn, seed=seed, drive_scale=drive, record_raster=False, raster_budget_bytes=budget)
+    if a.block_threads:
+        net.set_block_threads(a.block_threads)
     schemes = None
     if not a.no_schemes:
         schemes = schemes_leg(g, net, nsyn, min(T, 500))
