@@ -46,7 +46,8 @@
 //             contiguous run of sectors instead of two half-used ones: at 7,000 spikes per
 //             step this cut the delivery by a third (the step is bound by the sectors in
 //             flight per SM, not by the bytes).  Flat mapping (at least kFlatMinSpikes
-//             staged spikes, at most kFlatMax synapses for the rank): the segment bounds
+//             staged spikes, at most kFlatMax synapses for the rank, and, in a 768-thread
+//             CTA, fewer than NT/2 spikes): the segment bounds
 //             of all spikes at once, a block scan, every synapse of the concatenation
 //             mapped to its spike in shared memory, and thread i walks synapses i, i+NT,
 //             ... with eight reads in flight.  Run mapping (otherwise): a warp takes 32
@@ -517,7 +518,9 @@ __device__ void team_run(const TeamItem &it, int rank, unsigned char *s_raw, Tea
         __syncthreads();
         if (sh.fail) return;
       }
-      if (!solo && !gl && K >= kFlatMinSpikes && L.flat && K <= 4 * NT) {
+      // (a smaller CTA takes the flat mapping only for steps too small to give most of its
+      // warps a 32-spike batch of the run mapping, which measured faster above that)
+      if (!solo && !gl && K >= kFlatMinSpikes && L.flat && K <= 4 * NT && (NT >= 1024 || K < NT / 2)) {
         // segment bounds and their offsets in the concatenation (for the flat delivery):
         // thread t takes spikes 4t .. 4t+3 (K <= 4 NT); a block scan of their
         // lengths (every warp scans the warp sums itself), then each thread marks the
