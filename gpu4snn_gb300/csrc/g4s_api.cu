@@ -64,6 +64,10 @@ struct TeamLaunch {
   cudaGraphExec_t exec = nullptr;
   std::vector<uint64_t> sig;
   std::vector<int> order;  // networks of the round in flight (team_round_start .. finish)
+  TeamLaunch() = default;
+  TeamLaunch(const TeamLaunch &) = delete;
+  TeamLaunch &operator=(const TeamLaunch &) = delete;
+  ~TeamLaunch() { release(); }  // (a thread's own launch buffers go when the thread ends)
   void drop_graph() {
     if (exec) cudaGraphExecDestroy(exec);
     exec = nullptr;
@@ -80,7 +84,13 @@ struct TeamLaunch {
     cudaFreeHost(h_status);
     if (e0) cudaEventDestroy(e0);
     if (e1) cudaEventDestroy(e1);
-    *this = TeamLaunch{};
+    d_items = h_items = nullptr;
+    d_slots = h_slots = nullptr;
+    d_ctl = h_ctl = nullptr;
+    h_status = nullptr;
+    cap_items = cap_slots = 0;
+    e0 = e1 = nullptr;
+    order.clear();
   }
   int reserve(int items, int slots) {
     if (!e0 && (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess))
@@ -94,6 +104,7 @@ struct TeamLaunch {
       cudaFreeHost(h_status);
       d_items = h_items = nullptr;
       h_status = nullptr;
+      cap_items = 0;  // (until the new buffers exist)
       if (cudaMalloc((void **)&d_items, sizeof(TeamItem) * items) != cudaSuccess ||
           cudaMallocHost((void **)&h_items, sizeof(TeamItem) * items) != cudaSuccess ||
           cudaMallocHost((void **)&h_status, sizeof(int) * 2 * items) != cudaSuccess)
@@ -105,6 +116,7 @@ struct TeamLaunch {
       cudaFree(d_slots);
       cudaFreeHost(h_slots);
       d_slots = h_slots = nullptr;
+      cap_slots = 0;
       if (cudaMalloc((void **)&d_slots, sizeof(int2) * slots) != cudaSuccess ||
           cudaMallocHost((void **)&h_slots, sizeof(int2) * slots) != cudaSuccess)
         return set_error(G4S_ERR_NOMEM, "team slots");
