@@ -501,7 +501,7 @@ static int resolve_alg(g4s_net *n, int alg) {
 
 // ---------------------------------------------------------------------------------------
 // Team geometry of one network for the SKL team kernel: p CTAs (at most the co-resident
-// count, one per SM), by default one per 128 neurons alone and one per 4096 in a batch,
+// count, one per SM), by default one per 128 neurons alone and one per 8192 in a batch,
 // and the currents plus the spike buffer of a slice within the shared-memory limit.
 // Returns false if the network does not fit or its tables break the exactness bound of
 // the split accumulation (the global-atomic persistent kernel is used instead).
@@ -516,7 +516,7 @@ static bool plan_team(g4s_net *n, int want, bool batch, int *p_out, int64_t *rc_
   }
   pmax = std::min(pmax, kMaxTeam);
   // alone, a network spreads over the GPU (one CTA per 128 neurons, up to one per SM); in a
-  // batch it takes one CTA per 4096 neurons, so that more networks run at once
+  // batch it takes one CTA per 8192 neurons, so that more networks run at once
   int64_t p = want > 0 ? want : (batch ? (v.n + kBatchSlice - 1) / kBatchSlice : (v.n + kSoloSlice - 1) / kSoloSlice);
   if (p < 1) p = 1;
   if (p > pmax) p = pmax;

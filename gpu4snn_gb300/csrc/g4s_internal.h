@@ -47,9 +47,9 @@ constexpr int64_t kAbcdSlice = 2048;           // ... keep a, b, c, d in shared 
 constexpr int64_t kSoloSlice = 128;            // neurons per CTA of a network running alone (at
                                                // most: it spreads over every SM; measured best from
                                                // N = 2500 to 10^6)
-constexpr int64_t kBatchSlice = 4096;          // neurons per CTA of a batched network (measured on the
-                                               // 256-network ensemble: 448 sims/s against 401 at 2048
-                                               // and 453 at 8192; served requests 40.6/s, 35.4, 39.0)
+constexpr int64_t kBatchSlice = 8192;          // neurons per CTA of a batched network (measured on the
+                                               // 256-network ensemble: 510 ms against 534 at 4096 and
+                                               // 824 at 16384; served requests 41.9/s, 40.1, 32.7)
 constexpr int kMaxTeam = 192;                  // CTAs of one team (three record slots per thread)
 constexpr int kMinWindow = 1024;               // spike ids a multi-CTA rank can stage per delivery window
 constexpr int kMaxWindow = 4096;
