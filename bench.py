@@ -206,11 +206,12 @@ ALG_LABEL = {0: "AP", 1: "N", 2: "S", 3: "AB", 4: "SKL", 5: "AUTO"}
 
 
 def schemes_leg(g, net, nsyn, steps):
-    """Each of the five schemes on the same network for `steps` steps (the simulation
-    continues from one scheme to the next; the dynamics are stationary)."""
+    """Each of the five schemes on the same network for `steps` steps, after a warm-up run
+    of the same length (which also captures the host-driven schemes' chunk graphs; the
+    simulation continues from one run to the next; the dynamics are stationary)."""
     out = {}
     for alg in (0, 1, 2, 3, 4):
-        net.run(20, alg)
+        net.run(steps, alg)
         net.run(steps, alg)
         inf = net.info()
         out[ALG_LABEL[alg]] = {"events_per_s": inf.last_run_spikes * nsyn / (inf.last_run_ms * 1e-3),
@@ -365,7 +366,7 @@ def main():
         net.set_block_threads(a.block_threads)
     schemes = None
     if not a.no_schemes:
-        schemes = schemes_leg(g, net, nsyn, min(T, 500))
+        schemes = schemes_leg(g, net, nsyn, min(T, 2048))
     tuned = None
     if alg == g.ALG_AUTO:
         talg, tteam, tus = net.autotune(min(T, 200))

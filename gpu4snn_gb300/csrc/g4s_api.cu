@@ -148,6 +148,15 @@ struct g4s_net {
   double *d_stats = nullptr;
   int64_t chunk_steps = 0;   // steps per chunk of the team kernel
   int64_t chunk_legacy = 0;  // steps per chunk of the other kernels (raster = spike list)
+  // chunks of the host-driven schemes as CUDA graphs: the chunk's first step (device word,
+  // set from pinned memory at each replay) and up to kStepGraphs captured chunks, keyed by
+  // scheme, length, last-chunk flag and launch shape
+  long long *d_t0 = nullptr, *h_t0 = nullptr;
+  struct StepGraph {
+    std::vector<uint64_t> key;
+    cudaGraphExec_t exec = nullptr;
+  };
+  std::vector<StepGraph> step_graphs;
   int64_t t_abs = 0;
   uint32_t tag_next = 0;  // record tags of the team kernel: never repeated for this handle's lists
   uint64_t serial = 0;    // creation number, unique in the process (keys the captured rounds)
@@ -202,6 +211,11 @@ static void free_net(g4s_net *n) {
     n->rstream = nullptr;
   }
   n->launch.release();  // its captured round refers to the buffers below
+  for (auto &gr : n->step_graphs)  // (and so do the captured chunks)
+    if (gr.exec) cudaGraphExecDestroy(gr.exec);
+  n->step_graphs.clear();
+  cudaFree(n->d_t0);
+  cudaFreeHost(n->h_t0);
   cudaFree(const_cast<int2 *>(v.pair));
   cudaFree(v.vu);
   cudaFree(v.abcd);
@@ -319,7 +333,7 @@ static int alloc_net(const g4s_net_desc *d, g4s_net **out) {
       (rc = dalloc(n, &v.counts, (size_t)cs, "counts")) || (rc = dalloc(n, &v.base, (size_t)cs, "offsets")) ||
       (rc = dalloc(n, &v.stamps, (size_t)cs * 2 + 2, "stamps")) || (rc = dalloc(n, &v.status, 1, "status")) ||
       (rc = dalloc(n, &n->gs, 1 + 2 * (size_t)kMaxTeam * kRecLines, "barrier and spike records")) ||
-      (rc = dalloc(n, &n->d_stats, 2, "stats"))) {
+      (rc = dalloc(n, &n->d_stats, 2, "stats")) || (rc = dalloc(n, &n->d_t0, 1, "chunk start"))) {
     free_net(n);
     return rc;
   }
@@ -328,7 +342,8 @@ static int alloc_net(const g4s_net_desc *d, g4s_net **out) {
       (e = cudaEventCreate(&n->ek0)) != cudaSuccess || (e = cudaEventCreate(&n->ek1)) != cudaSuccess ||
       (e = cudaMallocHost((void **)&n->h_counts, (size_t)cs * 4)) != cudaSuccess ||
       (e = cudaMallocHost((void **)&n->h_base, (size_t)cs * 8)) != cudaSuccess ||
-      (e = cudaMallocHost((void **)&n->h_stamps, ((size_t)cs * 2 + 2) * 8)) != cudaSuccess) {
+      (e = cudaMallocHost((void **)&n->h_stamps, ((size_t)cs * 2 + 2) * 8)) != cudaSuccess ||
+      (e = cudaMallocHost((void **)&n->h_t0, sizeof(long long))) != cudaSuccess) {
     free_net(n);
     return cuda_error(e, "stream/event/pinned allocation");
   }
@@ -934,26 +949,72 @@ static int run_net(g4s_net *n, int32_t steps, int32_t alg_in) {
     }
   }
   while (!team && remaining > 0) {
-    const int cs = (int)std::min<int64_t>(remaining, n->chunk_legacy);
+    // (host-driven chunks stay short enough for their graphs to instantiate quickly)
+    const int64_t chunk = alg == kAlgSKL ? n->chunk_legacy : std::min<int64_t>(n->chunk_legacy, kStepGraphSteps);
+    const int cs = (int)std::min<int64_t>(remaining, chunk);
     const bool last_chunk = remaining == cs;
-    {
+    if (alg == kAlgSKL) {
       G4S_CUDA(cudaMemsetAsync(v.counts, 0, (size_t)cs * sizeof(int), n->stream));
       G4S_CUDA(cudaMemsetAsync(v.stamps, 0, ((size_t)cs * 2 + 2) * 8, n->stream));
-      if (alg == kAlgSKL) G4S_CUDA(cudaMemsetAsync(n->gs, 0, sizeof(GridSync), n->stream));
+      G4S_CUDA(cudaMemsetAsync(n->gs, 0, sizeof(GridSync), n->stream));
       G4S_CUDA(cudaEventRecord(n->ek0, n->stream));
-      if (alg == kAlgSKL) {
-        G4S_CUDA(launch_persistent(v, n->t_abs, cs, last_chunk, n->gs, n->barrier_ns, n->shape.group,
-                                   n->barrier_stall, n->stream));
-        n->barrier_stall = 0;
-        launches += 1;
-      } else {
+      G4S_CUDA(launch_persistent(v, n->t_abs, cs, last_chunk, n->gs, n->barrier_ns, n->shape.group,
+                                 n->barrier_stall, n->stream));
+      n->barrier_stall = 0;
+      launches += 1;
+      G4S_CUDA(cudaEventRecord(n->ek1, n->stream));
+    } else {
+      // The chunk as a CUDA graph (two launches per step would otherwise each cost a host
+      // launch and a gap on the GPU): the chunk's first step from pinned memory, the
+      // clears, then update and delivery for every step between two timing events.  A
+      // chunk is captured only when its graph will be replayed (a graph of this shape
+      // exists, or at least two more chunks of its length follow); otherwise it is
+      // launched step by step.
+      *n->h_t0 = n->t_abs;
+      const std::vector<uint64_t> key = {(uint64_t)alg, (uint64_t)cs, (uint64_t)last_chunk,
+                                         (uint64_t)n->shape.group, (uint64_t)n->shape.blocks_per_sm,
+                                         (uint64_t)n->shape.k_hint};
+      cudaGraphExec_t exec = nullptr;
+      for (auto &gr : n->step_graphs)
+        if (gr.key == key) exec = gr.exec;
+      const bool replayed = exec || (!last_chunk && remaining >= 2 * (int64_t)cs);
+      if (!replayed) {
+        G4S_CUDA(cudaMemcpyAsync(n->d_t0, n->h_t0, sizeof(long long), cudaMemcpyHostToDevice, n->stream));
+        G4S_CUDA(cudaMemsetAsync(v.counts, 0, (size_t)cs * sizeof(int), n->stream));
+        G4S_CUDA(cudaMemsetAsync(v.stamps, 0, ((size_t)cs * 2 + 2) * 8, n->stream));
+        G4S_CUDA(cudaEventRecord(n->ek0, n->stream));
         for (int lt = 0; lt < cs; ++lt) {
-          G4S_CUDA(launch_update(v, n->t_abs, lt, last_chunk && lt == cs - 1, n->stream));
+          G4S_CUDA(launch_update(v, n->d_t0, lt, last_chunk && lt == cs - 1, n->stream));
           G4S_CUDA(launch_deliver(v, lt, alg, n->shape, n->stream));
         }
-        launches += 2 * (int64_t)cs;
+        G4S_CUDA(cudaEventRecord(n->ek1, n->stream));
+      } else if (!exec) {
+        if ((int)n->step_graphs.size() >= kStepGraphs) {  // the oldest goes
+          cudaGraphExecDestroy(n->step_graphs.front().exec);
+          n->step_graphs.erase(n->step_graphs.begin());
+        }
+        G4S_CUDA(cudaStreamBeginCapture(n->stream, cudaStreamCaptureModeThreadLocal));
+        cudaError_t e = cudaMemcpyAsync(n->d_t0, n->h_t0, sizeof(long long), cudaMemcpyHostToDevice, n->stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(v.counts, 0, (size_t)cs * sizeof(int), n->stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(v.stamps, 0, ((size_t)cs * 2 + 2) * 8, n->stream);
+        if (e == cudaSuccess) e = cudaEventRecordWithFlags(n->ek0, n->stream, cudaEventRecordExternal);
+        for (int lt = 0; lt < cs && e == cudaSuccess; ++lt) {
+          e = launch_update(v, n->d_t0, lt, last_chunk && lt == cs - 1, n->stream);
+          if (e == cudaSuccess) e = launch_deliver(v, lt, alg, n->shape, n->stream);
+        }
+        if (e == cudaSuccess) e = cudaEventRecordWithFlags(n->ek1, n->stream, cudaEventRecordExternal);
+        cudaGraph_t g = nullptr;
+        const cudaError_t e_end = cudaStreamEndCapture(n->stream, &g);
+        if (e == cudaSuccess) e = e_end;
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, g, 0);
+        if (g) cudaGraphDestroy(g);
+        if (e != cudaSuccess) return cuda_error(e, "capturing a chunk of the step kernels");
+        n->step_graphs.push_back({key, exec});
       }
-      G4S_CUDA(cudaEventRecord(n->ek1, n->stream));
+      if (exec) G4S_CUDA(cudaGraphLaunch(exec, n->stream));
+      launches += 2 * (int64_t)cs;
+    }
+    {
       int rc = check_status(n, alg == kAlgSKL ? "persistent step kernel" : "step kernels");
       if (rc) return rc;
       float kms = 0.0f;

@@ -29,7 +29,8 @@ struct DeliverShape {
 
 cudaError_t launch_init(const NetView &v, cudaStream_t s);
 cudaError_t launch_conngen(const NetView &v, int self_loops, cudaStream_t s);
-cudaError_t launch_update(const NetView &v, int64_t t_abs0, int lt, bool last, cudaStream_t s);
+// t0: device word holding the absolute step of the chunk's step 0
+cudaError_t launch_update(const NetView &v, const long long *t0, int lt, bool last, cudaStream_t s);
 cudaError_t launch_deliver(const NetView &v, int lt, int alg, const DeliverShape &sh, cudaStream_t s);
 cudaError_t launch_persistent(const NetView &v, int64_t t_abs0, int nsteps, bool last_chunk, GridSync *gs,
                               unsigned long long limit_ns, int group, int stall, cudaStream_t s);
@@ -50,6 +51,8 @@ constexpr int64_t kSoloSlice = 128;            // neurons per CTA of a network r
 constexpr int64_t kBatchSlice = 8192;          // neurons per CTA of a batched network (measured on the
                                                // 256-network ensemble: 510 ms against 534 at 4096 and
                                                // 824 at 16384; served requests 41.9/s, 40.1, 32.7)
+constexpr int kStepGraphSteps = 512;          // longest chunk of the host-driven schemes (one CUDA graph)
+constexpr int kStepGraphs = 4;                 // captured chunks kept per network
 constexpr int kMaxTeam = 192;                  // CTAs of one team (three record slots per thread)
 constexpr int kMinWindow = 1024;               // spike ids a multi-CTA rank can stage per delivery window
 constexpr int kMaxWindow = 4096;

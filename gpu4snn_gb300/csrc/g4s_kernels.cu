@@ -176,8 +176,11 @@ __device__ __forceinline__ void update_phase(const NetView &v, int lt, int64_t t
   }
 }
 
+// (the chunk's first step is read from device memory, so that a captured chunk replays for
+// any chunk of the run)
 template <int NT>
-__global__ void __launch_bounds__(NT) k_update(NetView v, int64_t t_abs0, int lt, int last) {
+__global__ void __launch_bounds__(NT) k_update(NetView v, const long long *t0, int lt, int last) {
+  const int64_t t_abs0 = *t0;
   __shared__ int s_warp[NT / 32 + 1];
   __shared__ long long s_slot;
   const long long base_t = lt == 0 ? 0ll : __ldcg(v.base + lt - 1) + __ldcg(v.counts + lt - 1);
@@ -389,8 +392,8 @@ cudaError_t launch_conngen(const NetView &v, int self_loops, cudaStream_t s) {
 constexpr int kUpdNT = 256;
 constexpr int kPerNT = 512;
 
-cudaError_t launch_update(const NetView &v, int64_t t_abs0, int lt, bool last, cudaStream_t s) {
-  k_update<kUpdNT><<<grid_for(v.n, kUpdNT, 8), kUpdNT, 0, s>>>(v, t_abs0, lt, last ? 1 : 0);
+cudaError_t launch_update(const NetView &v, const long long *t0, int lt, bool last, cudaStream_t s) {
+  k_update<kUpdNT><<<grid_for(v.n, kUpdNT, 8), kUpdNT, 0, s>>>(v, t0, lt, last ? 1 : 0);
   return cudaGetLastError();
 }
 
