@@ -131,7 +131,7 @@ struct TuneChoice {
   int alg = kAlgSKL;
   int team = 0;
   int mode = kDeliverRun;
-  int nt = kTeamNT;  // threads per CTA of the team kernel
+  int nt = 0;  // threads per CTA of the team kernel (0: chosen from the step size)
 };
 
 // ---------------------------------------------------------------------------------------
@@ -190,7 +190,8 @@ struct g4s_net {
   size_t seg_bytes = 0;
   int want_p = 0;
   int deliver_mode = kDeliverRun;
-  int team_nt = kTeamNT;  // threads per CTA of its team rounds (kTeamNT or kTeamNTSmall)
+  int team_nt = 0;            // threads per CTA asked for: kTeamNT, kTeamNTSmall, 0 = automatic
+  int team_nt_eff = kTeamNT;  // ... in use (set when the team is planned)
   bool tables_fit = false;
   unsigned long long max_in = 0, max_mag = 0;
   TeamLaunch launch;
@@ -509,7 +510,10 @@ static int resolve_alg(g4s_net *n, int alg) {
   }
   if (c.alg == kAlgSKL) {
     n->deliver_mode = c.mode;
-    n->team_nt = c.nt;
+    if (n->team_nt != c.nt) {
+      n->team_nt = c.nt;
+      n->team_ready = false;
+    }
   }
   return c.alg;
 }
@@ -525,7 +529,8 @@ static bool plan_team(g4s_net *n, int want, bool batch, int *p_out, int64_t *rc_
   const NetView &v = n->v;
   if (!n->tables_fit) return false;
   int pmax = 0;
-  if (team_max_blocks(kTeamSmemLimit, &pmax, n->team_nt) != cudaSuccess || pmax < 1) {
+  // (both CTA sizes fit one CTA per SM: planned with the default)
+  if (team_max_blocks(kTeamSmemLimit, &pmax) != cudaSuccess || pmax < 1) {
     (void)cudaGetLastError();
     return false;
   }
@@ -542,7 +547,7 @@ static bool plan_team(g4s_net *n, int want, bool batch, int *p_out, int64_t *rc_
     if (team_smem(rc, (int)p) == 0) return false;
   }
   int pfit = 0;
-  if (team_max_blocks(team_smem(rc, (int)p), &pfit, n->team_nt) != cudaSuccess || pfit < p) {
+  if (team_max_blocks(team_smem(rc, (int)p), &pfit) != cudaSuccess || pfit < p) {
     (void)cudaGetLastError();
     return false;
   }
@@ -561,6 +566,16 @@ static int prepare_team(g4s_net *n, bool batch = false) {
   if (!plan_team(n, n->want_p, batch, &p, &rc)) {
     n->team_ok = false;
     return G4S_OK;
+  }
+  // CTA size: the one asked for; automatically 768 threads when a rank's expected share of
+  // a step is small (fewer than 32768 synapses, from the recent firing rate), where the
+  // spill-free kernel's shorter chain wins, else 1024 (more reads in flight); a batch takes
+  // 1024 (measured faster for ensembles of small networks)
+  if (n->team_nt) {
+    n->team_nt_eff = n->team_nt;
+  } else {
+    const double syn = (double)n->v.n * recent_rate(n) / 1000.0 * (double)n->v.nsyn / (double)p;
+    n->team_nt_eff = !batch && syn < 32768.0 ? kTeamNTSmall : kTeamNT;
   }
   // the interleaved rows of the team kernel's segment reads: optional (without them, as
   // when the device has no room left for them, the kernel reads the separate arrays)
@@ -773,9 +788,9 @@ static int team_round_start(g4s_net *const *nets, const int *steps, const bool *
   if (rc) return rc;
   bool pair = true;  // every network of the round has its interleaved rows
   for (int i : order) pair = pair && nets[i]->v.pair != nullptr;
-  int nt = nets[order[0]]->team_nt;  // threads per CTA: the networks' own when they agree
+  int nt = nets[order[0]]->team_nt_eff;  // threads per CTA: the networks' own when they agree
   for (int i : order)
-    if (nets[i]->team_nt != nt) nt = kTeamNT;
+    if (nets[i]->team_nt_eff != nt) nt = kTeamNT;
   int gmax = 0;
   G4S_CUDA(team_max_blocks(smem, &gmax, nt));  // also raises the kernel's shared-memory ceiling
   if (gmax < maxteam) return set_error(G4S_ERR_CUDA, "team larger than the co-resident grid");
@@ -1397,8 +1412,8 @@ int g4s_net_set_geometry(g4s_net *n, int32_t owner_blocks, int32_t delivery) {
 
 int g4s_net_set_block_threads(g4s_net *n, int32_t threads) {
   if (!n) return set_error(G4S_ERR_INVALID, "null handle");
-  if (threads != kTeamNT && threads != kTeamNTSmall)
-    return set_error(G4S_ERR_INVALID, "threads must be 1024 or 768");
+  if (threads != 0 && threads != kTeamNT && threads != kTeamNTSmall)
+    return set_error(G4S_ERR_INVALID, "threads must be 1024, 768 or 0 (automatic)");
   n->team_nt = threads;
   n->team_ready = false;
   n->team_ok = true;
@@ -1407,7 +1422,9 @@ int g4s_net_set_block_threads(g4s_net *n, int32_t threads) {
 
 int g4s_net_get_block_threads(g4s_net *n, int32_t *threads) {
   if (!n || !threads) return set_error(G4S_ERR_INVALID, "null argument");
-  *threads = n->team_nt;
+  const int rc = prepare_team(n);
+  if (rc) return rc;
+  *threads = n->team_nt_eff;
   return G4S_OK;
 }
 

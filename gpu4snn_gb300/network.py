@@ -94,7 +94,8 @@ class Network:
         check(load().g4s_net_set_geometry(self._h, owner_blocks, delivery))
 
     def set_block_threads(self, threads: int):
-        """Threads per CTA of the SKL team kernel: 1024 (default) or 768 (same results)."""
+        """Threads per CTA of the SKL team kernel: 1024, 768 or 0 (automatic, the default);
+        results do not depend on it."""
         check(load().g4s_net_set_block_threads(self._h, threads))
 
     def block_threads(self) -> int:

@@ -127,10 +127,12 @@ int g4s_net_set_barrier_timeout(g4s_net *net, uint64_t ns);
  * exact-accumulation bound, and the global-atomic persistent kernel runs instead) and the
  * neurons per CTA. */
 int g4s_net_set_geometry(g4s_net *net, int32_t owner_blocks, int32_t delivery);
-/* Threads per CTA of the SKL team kernel: 1024 (the default: the most table reads in
- * flight, for steps with many synapses per CTA) or 768 (80 registers a thread instead of
- * 64, no spills: faster for steps whose work is small).  Results do not depend on it; the
- * autotuner tries both.  A no-alloc run and a batch of networks that disagree use 1024. */
+/* Threads per CTA of the SKL team kernel: 1024 (the most table reads in flight, for steps
+ * with many synapses per CTA), 768 (80 registers a thread instead of 64, no spills: faster
+ * for steps whose work is small) or 0 (the default: 768 when a CTA's expected share of a
+ * step, from the recent firing rate, is under 32768 synapses, else 1024; 1024 in a batch).
+ * Results do not depend on it; the autotuner tries both sizes.  A no-alloc run and a batch
+ * of networks that disagree use 1024.  get_block_threads reports the size in use. */
 int g4s_net_set_block_threads(g4s_net *net, int32_t threads);
 int g4s_net_get_block_threads(g4s_net *net, int32_t *threads);
 int g4s_net_get_geometry(g4s_net *net, int32_t *owner_blocks, int64_t *slice);
