@@ -188,6 +188,24 @@ def test_block_threads_768_same_results(g4s, n, drive, p, mode):
     assert np.array_equal(ra, rb) and np.array_equal(va, vb) and np.array_equal(ca, cb)
 
 
+def test_block_threads_automatic_choice(g4s):
+    """Untuned, the team kernel's CTA size follows the expected synapses per CTA and step
+    (N=100,000 at ~8 Hz: ~5,000, under 32,768, so 768 threads); a size that is set stays,
+    0 restores the automatic choice, other sizes are refused."""
+    from gpu4snn_gb300 import _lib
+    with g4s.Network(100_000, 1000, seed=2, record_raster=False) as net:
+        assert net.block_threads() == 768
+        net.set_block_threads(1024)
+        assert net.block_threads() == 1024
+        net.run(20, 4)
+        assert net.block_threads() == 1024
+        net.set_block_threads(0)
+        assert net.block_threads() == 768
+        with pytest.raises(g4s.G4SError) as e:
+            net.set_block_threads(512)
+        assert e.value.code == _lib.ERR_INVALID
+
+
 def test_uploaded_tables_with_holes(g4s, oracle):
     """Caller tables may leave slots unused (negative target) anywhere in a row."""
     n, nsyn, seed = 3000, 200, 8
