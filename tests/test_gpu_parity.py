@@ -113,6 +113,23 @@ def test_chunked_run_matches(g4s, oracle):
             compare_state(net, sim)
 
 
+@pytest.mark.parametrize("alg", [0, 1, 2, 3])
+def test_host_driven_chunk_graphs(g4s, oracle, alg):
+    """The host-driven schemes run their 512-step chunks as CUDA graphs, replayed for every
+    chunk (the chunk's first step read from device memory): two runs of 1200 steps (captured
+    chunks, replays, a last chunk launched step by step) equal the oracle's 2400 steps."""
+    n, nsyn, seed = 1000, 100, 9
+    d, (idx, w) = oracle_tables(oracle, n, nsyn, seed)
+    sim = oracle.Sim(d, idx, w)
+    sim.run(2400, threads=8)
+    with g4s.Network(n, nsyn, seed=seed) as net:
+        net.run(1200, alg)
+        net.run(1200, alg)
+        assert net.info().steps_done == 2400
+        assert np.array_equal(np.stack(net.raster()), np.stack(sim.raster()))
+        compare_state(net, sim)
+
+
 def test_glibc_tables_on_gpu(g4s, oracle):
     n, nsyn, seed = 2500, 1000, 3
     idx, w = oracle.conn_glibc(seed, n, nsyn)
