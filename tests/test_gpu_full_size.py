@@ -1,0 +1,47 @@
+"""Parity at the full network sizes, where the oracle would take hours: properties that do
+not depend on size.  Every scheme accumulates the same Q32.32 integers, so the team kernel
+at both CTA sizes and the host-driven schemes must produce bit-identical rasters, states
+and pending currents; and every raster must be well formed (per-step counts that add up,
+ids in range and ascending within each step)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _run(g4s, n, nsyn, seed, steps, alg, threads=0):
+    with g4s.Network(n, nsyn, seed=seed, record_raster=True) as net:
+        if threads:
+            net.set_block_threads(threads)
+        net.run(steps, alg)
+        t, i = net.raster()
+        s = net.state()
+        return net.counts(), t, i, s["v"].view(np.uint32).copy(), s["u"].view(np.uint32).copy(), net.currents()
+
+
+def _well_formed(n, steps, counts, t, i):
+    assert len(counts) == steps and counts.sum() == len(t) == len(i)
+    assert np.all((i >= 0) & (i < n))
+    assert np.array_equal(t, np.repeat(np.arange(steps, dtype=np.int32), counts))
+    same_step = t[1:] == t[:-1]
+    assert np.all(i[1:][same_step] > i[:-1][same_step])  # ascending, no repeats, within a step
+
+
+ALL = [(4, 1024), (4, 768), (3, 0), (0, 0), (2, 0), (1, 0)]  # SKL at both CTA sizes, AB, AP, S, N
+
+
+@pytest.mark.parametrize("n,nsyn,steps", [
+    (1_000_000, 1000, 300),  # the N=10^6 configuration; 300 steps span two raster chunks
+    (250_000, 10_000, 100),  # 2.5e9 synapses
+])
+def test_full_size_schemes_agree(g4s, n, nsyn, steps):
+    ref = None
+    for alg, threads in ALL:
+        out = _run(g4s, n, nsyn, 3, steps, alg, threads)
+        _well_formed(n, steps, *out[:3])
+        assert out[0].sum() > steps * n // 2000  # the network fires (a few Hz at least)
+        if ref is None:
+            ref = out
+        else:
+            for a, b in zip(ref, out):
+                assert np.array_equal(a, b), (alg, threads)
