@@ -45,3 +45,21 @@ def test_full_size_schemes_agree(g4s, n, nsyn, steps):
         else:
             for a, b in zip(ref, out):
                 assert np.array_equal(a, b), (alg, threads)
+
+
+def test_full_size_table_round_trip(g4s):
+    """N=10^6 x 1000: the generated tables read back (8 GB) and uploaded to a second network
+    (validated on the host, found sorted, interleaved on the GPU) run identically."""
+    n, nsyn, seed, steps = 1_000_000, 1000, 3, 100
+    with g4s.Network(n, nsyn, seed=seed) as a:
+        idx, w = a.tables()
+        a.run(steps, 4)
+        ta, ia = a.raster()
+        va = a.state()["v"].view(np.uint32).copy()
+    with g4s.Network(n, nsyn, seed=seed, tables=(idx, w)) as b:
+        gi, gw = b.tables(0, 1000)
+        assert np.array_equal(gi, idx[:1000]) and np.array_equal(gw.view(np.uint32), w[:1000].view(np.uint32))
+        b.run(steps, 4)
+        tb, ib = b.raster()
+        assert np.array_equal(ta, tb) and np.array_equal(ia, ib)
+        assert np.array_equal(va, b.state()["v"].view(np.uint32))
