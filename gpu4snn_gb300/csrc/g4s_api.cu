@@ -627,13 +627,13 @@ static int prepare_team(g4s_net *n, bool batch = false) {
 // segment table of the team kernel is rebuilt on the next SKL run.  The exactness bound
 // of the split shared-memory accumulation is measured here: fewer than 65536 synapses
 // into any neuron and sum(|q| >> 16) + 1 over them below 2^31 - 2^20.
-static int finish_tables(g4s_net *n) {
+static int finish_tables(g4s_net *n, bool may_be_sorted) {
   // (rows that arrive sorted, as tables read back from a network do, skip the sort)
   int *flag = nullptr, h_unsorted = 1;
-  cudaError_t ef = cudaMalloc((void **)&flag, sizeof(int));
-  if (ef == cudaSuccess) ef = launch_rows_sorted(n->v, flag, n->stream);
-  if (ef == cudaSuccess) ef = cudaMemcpyAsync(&h_unsorted, flag, sizeof(int), cudaMemcpyDeviceToHost, n->stream);
-  if (ef == cudaSuccess) ef = cudaStreamSynchronize(n->stream);
+  cudaError_t ef = may_be_sorted ? cudaMalloc((void **)&flag, sizeof(int)) : cudaSuccess;
+  if (ef == cudaSuccess && flag) ef = launch_rows_sorted(n->v, flag, n->stream);
+  if (ef == cudaSuccess && flag) ef = cudaMemcpyAsync(&h_unsorted, flag, sizeof(int), cudaMemcpyDeviceToHost, n->stream);
+  if (ef == cudaSuccess && flag) ef = cudaStreamSynchronize(n->stream);
   cudaFree(flag);
   if (ef != cudaSuccess) return cuda_error(ef, "row order check");
   if (h_unsorted) G4S_CUDA(launch_sort_rows(n->v, n->stream));
@@ -1336,7 +1336,7 @@ int g4s_net_create(const g4s_net_desc *desc, g4s_net **out) {
     cudaError_t e = launch_conngen(n->v, desc->self_loops, n->stream);
     if (e != cudaSuccess) rc = cuda_error(e, "connectivity kernel");
     if (!rc) rc = check_status(n, "connectivity kernel");
-    if (!rc) rc = finish_tables(n);
+    if (!rc) rc = finish_tables(n, false);  // (generated rows are in draw order)
   }
   if (!rc) rc = reset_net(n);
   if (rc) {
@@ -1395,7 +1395,7 @@ int g4s_net_load_tables(g4s_net *n, const int32_t *idx, const float *w, int32_t 
   }
   G4S_CUDA(cudaMemcpyAsync(const_cast<int *>(v.idx), idx, bytes, cudaMemcpyHostToDevice, n->stream));
   G4S_CUDA(cudaMemcpyAsync(const_cast<float *>(v.w), w, bytes, cudaMemcpyHostToDevice, n->stream));
-  return finish_tables(n);
+  return finish_tables(n, true);
 }
 
 int g4s_net_set_geometry(g4s_net *n, int32_t owner_blocks, int32_t delivery) {

@@ -108,14 +108,22 @@ __global__ void k_sort_rows(NetView v, int p2) {
 
 // Rows already in the sort's order (ascending 64-bit keys target << 32 | weight bits, the
 // targets taken as unsigned so that unused slots come last)?  *unsorted = 1 if not.
+// One warp per row, consecutive lanes on consecutive slots.
 __global__ void k_rows_sorted(NetView v, int *unsorted) {
-  const int64_t total = v.n * (int64_t)v.stride;
-  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < total; g += (int64_t)gridDim.x * blockDim.x) {
-    if ((g + 1) % v.stride == 0) continue;  // the last slot of a row
-    const unsigned long long a = ((unsigned long long)(unsigned)v.idx[g] << 32) | __float_as_uint(v.w[g]);
-    const unsigned long long b = ((unsigned long long)(unsigned)v.idx[g + 1] << 32) | __float_as_uint(v.w[g + 1]);
-    if (a > b) *unsorted = 1;
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  bool bad = false;
+  for (int64_t row = warp; row < v.n; row += nwarps) {
+    const int *ri = v.idx + row * v.stride;
+    const float *rw = v.w + row * v.stride;
+    for (int j = lane; j + 1 < v.stride; j += 32) {
+      const unsigned long long a = ((unsigned long long)(unsigned)ri[j] << 32) | __float_as_uint(rw[j]);
+      const unsigned long long b = ((unsigned long long)(unsigned)ri[j + 1] << 32) | __float_as_uint(rw[j + 1]);
+      bad |= a > b;
+    }
   }
+  if (__any_sync(0xFFFFFFFFu, bad) && lane == 0) *unsorted = 1;
 }
 
 // Segment table: seg[row][k] = first slot of the sorted row whose target is >= k*Rc, for
