@@ -636,7 +636,7 @@ static int finish_tables(g4s_net *n, bool may_be_sorted) {
   if (ef == cudaSuccess && flag) ef = cudaStreamSynchronize(n->stream);
   cudaFree(flag);
   if (ef != cudaSuccess) return cuda_error(ef, "row order check");
-  if (h_unsorted) G4S_CUDA(launch_sort_rows(n->v, n->stream));
+  if (h_unsorted) G4S_CUDA(launch_sort_rows(n->v, !may_be_sorted, n->stream));
   n->team_ready = false;
   n->pair_ready = false;
   unsigned *cnt = nullptr;

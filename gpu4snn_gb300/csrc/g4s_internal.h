@@ -129,7 +129,10 @@ inline int team_window(int64_t rc, int team) {
   const size_t cap = (kTeamSmemLimit - base) / kPerId;
   return (int)(cap > (size_t)kMaxWindow ? kMaxWindow : cap & ~(size_t)7);
 }
-cudaError_t launch_sort_rows(const NetView &v, cudaStream_t s);
+// Rows sorted by target (unsigned, so unused slots last), equal targets by weight bits;
+// generated = rows as the connectivity kernel writes them (distinct targets, unused slots
+// (-1, 0.0f)), which a narrower key sorts into the same order.
+cudaError_t launch_sort_rows(const NetView &v, bool generated, cudaStream_t s);
 // *unsorted <- 1 if some row is not in launch_sort_rows' order, else 0
 cudaError_t launch_rows_sorted(const NetView &v, int *unsorted, cudaStream_t s);
 cudaError_t launch_segoff(const NetView &v, int team, int64_t rc, uint16_t *seg, cudaStream_t s);

@@ -61,6 +61,7 @@
 //   The raster records the spike ids of every step while its buffer has room.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 
 #include "g4s_device.cuh"
@@ -70,39 +71,152 @@ namespace g4s {
 
 // ---------------------------------------------------------------------------------------
 // Row sort: every row's (target, weight) pairs in ascending target order, unused slots
-// (negative targets, i.e. huge as unsigned) last.  One CTA per row, bitonic network over
-// 64-bit keys (target << 32 | weight bits) in shared memory.
+// (negative targets, i.e. huge as unsigned) last.  One CTA of NT threads per row, a bitonic
+// network over p2 = E * NT 64-bit keys (target << 32 | weight bits); thread t holds the
+// keys of elements t, t + NT, ..., in registers.  A compare-exchange over distance j takes
+// place in registers when j >= NT (the partner is the same thread's), through shuffles
+// when j < 32 (the partner is in the same warp), and through shared memory between warps
+// otherwise, so that only those stages need block barriers.
 // ---------------------------------------------------------------------------------------
-__global__ void k_sort_rows(NetView v, int p2) {
+template <int E>
+__global__ void __launch_bounds__(1024) k_sort_rows(NetView v, int p2) {
   extern __shared__ unsigned long long s_key[];
+  const int NT = blockDim.x, t = threadIdx.x;
   for (int64_t row = blockIdx.x; row < v.n; row += gridDim.x) {
     int *ri = const_cast<int *>(v.idx) + row * v.stride;
     float *rw = const_cast<float *>(v.w) + row * v.stride;
-    for (int j = threadIdx.x; j < p2; j += blockDim.x)
-      s_key[j] = j < v.stride ? ((unsigned long long)(unsigned)ri[j] << 32) | __float_as_uint(rw[j])
-                              : 0xFFFFFFFFFFFFFFFFull;
-    __syncthreads();
+    unsigned long long key[E];
+#pragma unroll
+    for (int r = 0; r < E; ++r) {
+      const int e = r * NT + t;
+      key[r] = e < v.stride ? ((unsigned long long)(unsigned)ri[e] << 32) | __float_as_uint(rw[e])
+                            : 0xFFFFFFFFFFFFFFFFull;
+    }
     for (int k = 2; k <= p2; k <<= 1)
       for (int j = k >> 1; j > 0; j >>= 1) {
-        for (int i = threadIdx.x; i < p2; i += blockDim.x) {
-          const int l = i ^ j;
-          if (l > i) {
-            const unsigned long long a = s_key[i], b = s_key[l];
-            const bool up = (i & k) == 0;
-            if ((a > b) == up) {
-              s_key[i] = b;
-              s_key[l] = a;
+        if (j >= NT) {
+          const int rj = j / NT;
+#pragma unroll
+          for (int RJ = 1; RJ < E; RJ <<= 1)  // (each distance unrolled: registers, not memory)
+            if (rj == RJ) {
+#pragma unroll
+              for (int r = 0; r < E; ++r)
+                if ((r & RJ) == 0) {
+                  const bool asc = ((r * NT + t) & k) == 0;
+                  const unsigned long long a = key[r], b = key[r | RJ];
+                  if ((a > b) == asc) {
+                    key[r] = b;
+                    key[r | RJ] = a;
+                  }
+                }
+            }
+        } else {
+          if (j >= 32) {
+            __syncthreads();  // (the previous stage's reads are done)
+#pragma unroll
+            for (int r = 0; r < E; ++r) s_key[r * NT + t] = key[r];
+            __syncthreads();
+          }
+#pragma unroll
+          for (int r = 0; r < E; ++r) {
+            const int e = r * NT + t;
+            const unsigned long long o = j >= 32 ? s_key[e ^ j] : __shfl_xor_sync(0xFFFFFFFFu, key[r], j);
+            const bool keep_min = ((e & j) == 0) == ((e & k) == 0);
+            key[r] = keep_min ? (o < key[r] ? o : key[r]) : (o > key[r] ? o : key[r]);
+          }
+        }
+      }
+#pragma unroll
+    for (int r = 0; r < E; ++r) {
+      const int e = r * NT + t;
+      if (e < v.stride) {
+        ri[e] = (int)(key[r] >> 32);
+        rw[e] = __uint_as_float((unsigned)key[r]);
+      }
+    }
+  }
+}
+
+// Generated rows (distinct targets, every unused slot (-1, 0.0f)) in the same order as
+// k_sort_rows' by narrower keys: 32-bit key target << pb | slot (n << pb | slot for an
+// unused slot), 2^pb >= p2 and (n << pb) + p2 - 1 below 2^32 - 1, so that every key names
+// the slot its pair comes from and only the keys are sorted.  The row is read once into
+// shared memory (targets, weights), sorted as E consecutive keys a thread (compare-
+// exchanges within a thread below distance E, shuffles below 32E, shared memory above)
+// and written back by gathering each sorted key's pair from the shared copy.
+template <int E>
+__global__ void __launch_bounds__(1024) k_sort_gen(NetView v, int p2, int pb) {
+  extern __shared__ __align__(16) unsigned s_gen[];
+  const int NT = blockDim.x, t = threadIdx.x;
+  unsigned *s_key = s_gen;                                // p2 keys
+  int *s_i = reinterpret_cast<int *>(s_gen + p2);         // the row's targets
+  float *s_w = reinterpret_cast<float *>(s_i + v.stride);  // the row's weights
+  const unsigned n = (unsigned)v.n, smask = (unsigned)p2 - 1u;
+  for (int64_t row = blockIdx.x; row < v.n; row += gridDim.x) {
+    int *ri = const_cast<int *>(v.idx) + row * v.stride;
+    float *rw = const_cast<float *>(v.w) + row * v.stride;
+    for (int e = t; e < v.stride; e += NT) {
+      s_i[e] = ri[e];
+      s_w[e] = rw[e];
+    }
+    __syncthreads();
+    unsigned key[E];
+#pragma unroll
+    for (int r = 0; r < E; ++r) {
+      const int e = t * E + r;
+      const unsigned ti = e < v.stride ? (unsigned)s_i[e] : 0u;
+      key[r] = e < v.stride ? ((ti < n ? ti : n) << pb) | (unsigned)e : 0xFFFFFFFFu;
+    }
+    for (int k = 2; k <= p2; k <<= 1)
+      for (int j = k >> 1; j > 0; j >>= 1) {
+        if (j < E) {
+#pragma unroll
+          for (int J = 1; J < E; J <<= 1)  // (each distance unrolled: registers, not memory)
+            if (j == J) {
+#pragma unroll
+              for (int r = 0; r < E; ++r)
+                if ((r & J) == 0) {
+                  const bool asc = ((t * E + r) & k) == 0;
+                  const unsigned a = key[r], b = key[r | J];
+                  const unsigned lo = a < b ? a : b, hi = a < b ? b : a;
+                  key[r] = asc ? lo : hi;
+                  key[r | J] = asc ? hi : lo;
+                }
+            }
+        } else {
+          // distance j >= E: the partner of slot t*E + r is slot (t ^ j/E)*E + r
+          const int tj = j / E;
+          const bool keep_min = ((t & tj) == 0) == (((t * E) & k) == 0);
+          if (tj < 32) {
+#pragma unroll
+            for (int r = 0; r < E; ++r) {
+              const unsigned o = __shfl_xor_sync(0xFFFFFFFFu, key[r], tj);
+              key[r] = keep_min ? (o < key[r] ? o : key[r]) : (o > key[r] ? o : key[r]);
+            }
+          } else {
+            __syncthreads();  // (the previous exchange's reads are done)
+#pragma unroll
+            for (int r = 0; r < E; ++r) s_key[t * E + r] = key[r];
+            __syncthreads();
+            const unsigned *src = s_key + (t ^ tj) * E;
+#pragma unroll
+            for (int r = 0; r < E; ++r) {
+              const unsigned o = src[r];
+              key[r] = keep_min ? (o < key[r] ? o : key[r]) : (o > key[r] ? o : key[r]);
             }
           }
         }
-        __syncthreads();
       }
-    for (int j = threadIdx.x; j < v.stride; j += blockDim.x) {
-      const unsigned long long x = s_key[j];
-      ri[j] = (int)(x >> 32);
-      rw[j] = __uint_as_float((unsigned)x);
-    }
     __syncthreads();
+#pragma unroll
+    for (int r = 0; r < E; ++r) s_key[t * E + r] = key[r];
+    __syncthreads();
+    for (int e = t; e < v.stride; e += NT) {
+      const unsigned from = s_key[e] & smask;  // (the first stride keys are the row's own)
+      ri[e] = s_i[from];
+      rw[e] = s_w[from];
+    }
+    __syncthreads();  // (before the next row overwrites the shared copy)
   }
 }
 
@@ -887,26 +1001,70 @@ cudaError_t launch_rows_sorted(const NetView &v, int *unsorted, cudaStream_t s) 
   return cudaGetLastError();
 }
 
-cudaError_t launch_sort_rows(const NetView &v, cudaStream_t s) {
-  int p2 = 32;
-  while (p2 < v.stride) p2 <<= 1;
-  const size_t smem = (size_t)p2 * 8;
-  if (smem > 200 * 1024) return cudaErrorInvalidValue;
-  // the ceiling is the same for every network, so that host threads sorting rows of
-  // different lengths never lower it under one another's launch
-  cudaError_t e = cudaFuncSetAttribute(k_sort_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+// One CTA per row, as many resident as fit (at most one per row).  The shared-memory
+// ceiling is the same for every network, so that host threads sorting rows of different
+// lengths never lower it under one another's launch.
+template <typename Kernel>
+static cudaError_t row_grid(Kernel kern, int nt, size_t smem, int64_t rows, unsigned *grid) {
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
   if (e != cudaSuccess) return e;
-  const int nt = p2 >= 4096 ? 1024 : (p2 >= 1024 ? 256 : 128);
   int occ = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_sort_rows, nt, smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, nt, smem);
   if (occ < 1) occ = 1;
   int dev = 0, sms = 1;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   int64_t g = (int64_t)sms * occ;
-  if (g > v.n) g = v.n;
-  k_sort_rows<<<(unsigned)g, nt, smem, s>>>(v, p2);
+  *grid = (unsigned)(g > rows ? rows : g);
+  return cudaSuccess;
+}
+
+template <int E>
+static cudaError_t sort_rows_e(const NetView &v, int p2, int nt, cudaStream_t s) {
+  const size_t smem = nt > 32 ? (size_t)p2 * 8 : 0;  // (one warp needs no shared memory)
+  unsigned g = 0;
+  cudaError_t e = row_grid(k_sort_rows<E>, nt, smem, v.n, &g);
+  if (e != cudaSuccess) return e;
+  k_sort_rows<E><<<g, nt, smem, s>>>(v, p2);
   return cudaGetLastError();
+}
+
+template <int E>
+static cudaError_t sort_gen_e(const NetView &v, int p2, int pb, cudaStream_t s) {
+  const int nt = p2 / E;
+  const size_t smem = (size_t)p2 * 4 + (size_t)v.stride * 8;
+  unsigned g = 0;
+  cudaError_t e = row_grid(k_sort_gen<E>, nt, smem, v.n, &g);
+  if (e != cudaSuccess) return e;
+  k_sort_gen<E><<<g, nt, smem, s>>>(v, p2, pb);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sort_rows(const NetView &v, bool generated, cudaStream_t s) {
+  int p2 = 32, pb = 5;
+  while (p2 < v.stride) p2 <<= 1, ++pb;
+  if ((size_t)p2 * 8 > 200 * 1024) return cudaErrorInvalidValue;
+  if (generated && ((uint64_t)v.n << pb) + (uint64_t)p2 - 1 < 0xFFFFFFFFull) {
+    // E consecutive keys a thread: 8 (up to 16 for rows longer than 8192), fewer for short rows
+    const int E = p2 / 32 < 8 ? p2 / 32 : (p2 / 8 > 1024 ? 16 : 8);
+    switch (E) {
+      case 1: return sort_gen_e<1>(v, p2, pb, s);
+      case 2: return sort_gen_e<2>(v, p2, pb, s);
+      case 4: return sort_gen_e<4>(v, p2, pb, s);
+      case 8: return sort_gen_e<8>(v, p2, pb, s);
+      case 16: return sort_gen_e<16>(v, p2, pb, s);
+      default: return cudaErrorInvalidValue;
+    }
+  }
+  const int nt = std::min(1024, std::max(32, p2 / 4));  // four keys a thread (up to 16 for long rows)
+  switch (p2 / nt) {
+    case 1: return sort_rows_e<1>(v, p2, nt, s);
+    case 2: return sort_rows_e<2>(v, p2, nt, s);
+    case 4: return sort_rows_e<4>(v, p2, nt, s);
+    case 8: return sort_rows_e<8>(v, p2, nt, s);
+    case 16: return sort_rows_e<16>(v, p2, nt, s);
+    default: return cudaErrorInvalidValue;
+  }
 }
 
 cudaError_t launch_segoff(const NetView &v, int team, int64_t rc, uint16_t *seg, cudaStream_t s) {

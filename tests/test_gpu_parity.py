@@ -44,6 +44,17 @@ def test_tables_large_sampled_rows(g4s, oracle):
             assert same_tables(gi, gw, oi, ow)
 
 
+def test_tables_long_sampled_rows(g4s, oracle):
+    """Rows of 10,000 synapses (the row sort's widest form: 16 keys per thread, 1024 threads)."""
+    n, nsyn, seed = 12_000, 10_000, 4
+    d = oracle.make_desc(n, nsyn, seed)
+    with g4s.Network(n, nsyn, seed=seed, record_raster=False) as net:
+        for row0 in (0, 5_999, n - 3):
+            gi, gw = net.tables(row0, 3)
+            oi, ow = oracle.conn_philox(d, row0, 3)
+            assert same_tables(gi, gw, oi, ow)
+
+
 def compare_state(net, sim):
     s, o = net.state(), sim.state()
     for k in ("v", "u", "a", "b", "c", "d"):
