@@ -52,11 +52,13 @@ __global__ void k_init_state(NetView v) {
 }
 
 // ---------------------------------------------------------------------------------------
-// Connectivity.  One warp per row keeps the row's accepted targets in a shared-memory
-// open-addressing set.  Draws are consumed in the order the oracle defines: block b, word
-// r, lane l is draw 128b + 32r + l.  Within one word round, a draw is fresh iff its target
-// is not in the set and no lower lane drew the same target (__match_any_sync); fresh draws
-// are accepted in lane order until the row holds nsyn targets.
+// Connectivity.  One warp per row keeps the row's accepted targets in a shared-memory set:
+// a bitmap of the n targets when that is the smaller (bits > 0 words), else an
+// open-addressing hash of 2^log2h ints.  Draws are consumed in the order the oracle
+// defines: block b, word r, lane l is draw 128b + 32r + l.  Within one word round, a draw
+// is fresh iff its target is not in the set and no lower lane drew the same target
+// (__match_any_sync: only the lowest such lane inserts); fresh draws are accepted in lane
+// order until the row holds nsyn targets.
 // ---------------------------------------------------------------------------------------
 __device__ __forceinline__ bool set_insert(int *set, unsigned mask, int log2h, int t) {
   unsigned h = ((unsigned)t * 0x9E3779B1u) >> (32 - log2h);
@@ -69,19 +71,26 @@ __device__ __forceinline__ bool set_insert(int *set, unsigned mask, int log2h, i
   return false;  // unreachable: the set is sized for twice the row plus one round
 }
 
-__global__ void k_conngen(NetView v, int self_loops, int log2h, int64_t row0, int64_t nrows,
+__device__ __forceinline__ bool bit_insert(int *bits, int t) {
+  const unsigned b = 1u << (t & 31);
+  return (atomicOr(reinterpret_cast<unsigned *>(bits) + (t >> 5), b) & b) == 0u;
+}
+
+__global__ void k_conngen(NetView v, int self_loops, int log2h, int bits, int64_t row0, int64_t nrows,
                           unsigned long long max_blocks) {
-  extern __shared__ int s_set[];
+  extern __shared__ __align__(16) int s_set[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
   const unsigned hsize = 1u << log2h, mask = hsize - 1;
-  int *set = s_set + (size_t)wib * hsize;
+  const unsigned words = bits > 0 ? (unsigned)bits : hsize;  // (a multiple of 4)
+  int *set = s_set + (size_t)wib * words;
+  const int fill = bits > 0 ? 0 : -1;
   const uint64_t range = self_loops ? (uint64_t)v.n : (uint64_t)(v.n - 1);
   const float wscale = __fdiv_rn(1000.0f, (float)v.nsyn);
   for (int64_t rr = (int64_t)blockIdx.x * wpb + wib; rr < nrows; rr += (int64_t)gridDim.x * wpb) {
     const int64_t row = row0 + rr;
     int *ri = const_cast<int *>(v.idx) + row * v.stride;
     float *rw = const_cast<float *>(v.w) + row * v.stride;
-    for (unsigned j = lane; j < hsize; j += 32) set[j] = -1;
+    for (unsigned j = lane; j < words / 4; j += 32) reinterpret_cast<int4 *>(set)[j] = make_int4(fill, fill, fill, fill);
     __syncwarp();
     int accepted = 0;
     for (unsigned long long b = 0; accepted < v.nsyn; ++b) {
@@ -98,7 +107,7 @@ __global__ void k_conngen(NetView v, int self_loops, int log2h, int64_t row0, in
         const unsigned same = __match_any_sync(0xFFFFFFFFu, ti);
         const bool leader = (__ffs(same) - 1) == lane;
         bool fresh = false;
-        if (leader) fresh = set_insert(set, mask, log2h, ti);
+        if (leader) fresh = bits > 0 ? bit_insert(set, ti) : set_insert(set, mask, log2h, ti);
         const unsigned fb = __ballot_sync(0xFFFFFFFFu, fresh);
         const int pos = accepted + __popc(fb & ((1u << lane) - 1u));
         if (fresh && pos < v.nsyn) ri[pos] = ti;
@@ -365,27 +374,30 @@ cudaError_t launch_init(const NetView &v, cudaStream_t s) {
 cudaError_t launch_conngen(const NetView &v, int self_loops, cudaStream_t s) {
   int log2h = 5;
   while ((1 << log2h) < 2 * v.nsyn + 64) ++log2h;
-  const size_t per_warp = (size_t)4 << log2h;
-  int wpb = (int)((96 * 1024) / per_warp);
-  if (wpb > 8) wpb = 8;
-  if (wpb < 1) wpb = 1;
-  const size_t smem = per_warp * wpb;
-  if (smem > 200 * 1024) return cudaErrorInvalidValue;
+  // the target bitmap (n bits, in 16-byte units) where it is smaller than the hash
+  const int64_t bm_words = ((v.n + 127) / 128) * 4;
+  const int bits = bm_words < ((int64_t)1 << log2h) ? (int)bm_words : 0;
+  const size_t per_warp = bits > 0 ? (size_t)4 * bits : (size_t)4 << log2h;
+  if (per_warp > 200 * 1024) return cudaErrorInvalidValue;
   // one ceiling for every network (concurrent host threads generating tables of different
   // fan-outs must not lower it under one another's launch)
   cudaError_t e = cudaFuncSetAttribute(k_conngen, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
   if (e != cudaSuccess) return e;
+  // warps per CTA (at most 8): the most resident warps per SM
+  int wpb = 1, best = 0, occ_best = 1;
+  for (int w = 1; w <= 8 && per_warp * w <= 200 * 1024; ++w) {
+    int occ = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_conngen, w * 32, per_warp * w);
+    if (occ * w > best) best = occ * w, wpb = w, occ_best = occ < 1 ? 1 : occ;
+  }
+  const size_t smem = per_warp * wpb;
   const uint64_t range = self_loops ? (uint64_t)v.n : (uint64_t)(v.n - 1);
   // generous cap on draw blocks (a full row needs about range * ln(range) draws)
   unsigned long long max_blocks = (64ull * (range + (uint64_t)v.nsyn) + 4096ull) / 128ull + 64ull;
-  int occ = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_conngen, wpb * 32, smem);
-  if (occ < 1) occ = 1;
-  const int64_t rows_per_block = wpb;
-  int64_t g = (v.n + rows_per_block - 1) / rows_per_block;
-  const int64_t cap = (int64_t)sm_count() * occ * 8;
+  int64_t g = (v.n + wpb - 1) / wpb;
+  const int64_t cap = (int64_t)sm_count() * occ_best * 8;
   if (g > cap) g = cap;
-  k_conngen<<<(unsigned)g, wpb * 32, smem, s>>>(v, self_loops, log2h, 0, v.n, max_blocks);
+  k_conngen<<<(unsigned)g, wpb * 32, smem, s>>>(v, self_loops, log2h, bits, 0, v.n, max_blocks);
   return cudaGetLastError();
 }
 

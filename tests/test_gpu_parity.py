@@ -34,11 +34,13 @@ def test_tables_bit_exact(g4s, oracle, n, nsyn, seed, self_loops):
     assert same_tables(gi, gw, idx, w)
 
 
-def test_tables_large_sampled_rows(g4s, oracle):
-    n, nsyn, seed = 100_000, 1000, 2
+@pytest.mark.parametrize("n,nsyn,seed", [(100_000, 1000, 2), (300_000, 1000, 6)])
+def test_tables_large_sampled_rows(g4s, oracle, n, nsyn, seed):
+    """Sampled rows of large tables: 100k x 1000 keeps each row's targets in a bitmap of the
+    n targets, 300k x 1000 in a hash set (the smaller of the two)."""
     d = oracle.make_desc(n, nsyn, seed)
     with g4s.Network(n, nsyn, seed=seed, record_raster=False) as net:
-        for row0 in (0, 1, 49_999, 79_999, 80_000, n - 3):
+        for row0 in (0, 1, n // 2 - 1, (n * 4) // 5 - 1, (n * 4) // 5, n - 3):
             gi, gw = net.tables(row0, 3)
             oi, ow = oracle.conn_philox(d, row0, 3)
             assert same_tables(gi, gw, oi, ow)
