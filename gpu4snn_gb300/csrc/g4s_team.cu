@@ -138,85 +138,97 @@ __global__ void __launch_bounds__(1024) k_sort_rows(NetView v, int p2) {
 }
 
 // Generated rows (distinct targets, every unused slot (-1, 0.0f)) in the same order as
-// k_sort_rows' by narrower keys: 32-bit key target << pb | slot (n << pb | slot for an
-// unused slot), 2^pb >= p2 and (n << pb) + p2 - 1 below 2^32 - 1, so that every key names
-// the slot its pair comes from and only the keys are sorted.  The row is read once into
-// shared memory (targets, weights), sorted as E consecutive keys a thread (compare-
-// exchanges within a thread below distance E, shuffles below 32E, shared memory above)
-// and written back by gathering each sorted key's pair from the shared copy.
+// k_sort_rows' by a bucket sort of narrower keys: 32-bit key target << pb | slot (n << pb
+// | slot for an unused slot), 2^pb >= p2 and (n << pb) + p2 - 1 below 2^32 - 1, unique, so
+// that every key names the slot its weight comes from.  Bucket of a key: its target >> sh
+// (targets taken as n for unused slots; n >> sh < nb), monotone in the key, about two to
+// four keys each as the targets are drawn uniformly.  Per row: the weights into shared
+// memory; a histogram whose atomics also give each key its rank in its bucket; a block
+// scan of the counts; each key stored at its bucket's start + its rank; one thread per
+// bucket orders the bucket's keys by insertion; the row written back (target from the
+// key, weight gathered from the shared copy).  E keys a thread, element r * NT + t.
 template <int E>
-__global__ void __launch_bounds__(1024) k_sort_gen(NetView v, int p2, int pb) {
+__global__ void __launch_bounds__(1024) k_sort_gen(NetView v, int pb, int nb, int sh) {
   extern __shared__ __align__(16) unsigned s_gen[];
-  const int NT = blockDim.x, t = threadIdx.x;
-  unsigned *s_key = s_gen;                                // p2 keys
-  int *s_i = reinterpret_cast<int *>(s_gen + p2);         // the row's targets
-  float *s_w = reinterpret_cast<float *>(s_i + v.stride);  // the row's weights
-  const unsigned n = (unsigned)v.n, smask = (unsigned)p2 - 1u;
+  const int NT = blockDim.x, t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  unsigned *s_cnt = s_gen;                                  // nb counts, then bucket starts
+  unsigned *s_part = s_cnt + nb;                            // 32 warp sums
+  unsigned *s_key = s_part + 32;                            // stride keys, by bucket
+  float *s_w = reinterpret_cast<float *>(s_key + v.stride);  // the row's weights
+  const unsigned n = (unsigned)v.n, smask = (1u << pb) - 1u, lim = n << pb;
+  const int per = nb / NT;  // buckets a thread scans (nb is a multiple of NT)
   for (int64_t row = blockIdx.x; row < v.n; row += gridDim.x) {
     int *ri = const_cast<int *>(v.idx) + row * v.stride;
     float *rw = const_cast<float *>(v.w) + row * v.stride;
-    for (int e = t; e < v.stride; e += NT) {
-      s_i[e] = ri[e];
-      s_w[e] = rw[e];
-    }
-    __syncthreads();
+    for (int b = t; b < nb; b += NT) s_cnt[b] = 0u;
     unsigned key[E];
 #pragma unroll
     for (int r = 0; r < E; ++r) {
-      const int e = t * E + r;
-      const unsigned ti = e < v.stride ? (unsigned)s_i[e] : 0u;
-      key[r] = e < v.stride ? ((ti < n ? ti : n) << pb) | (unsigned)e : 0xFFFFFFFFu;
-    }
-    for (int k = 2; k <= p2; k <<= 1)
-      for (int j = k >> 1; j > 0; j >>= 1) {
-        if (j < E) {
-#pragma unroll
-          for (int J = 1; J < E; J <<= 1)  // (each distance unrolled: registers, not memory)
-            if (j == J) {
-#pragma unroll
-              for (int r = 0; r < E; ++r)
-                if ((r & J) == 0) {
-                  const bool asc = ((t * E + r) & k) == 0;
-                  const unsigned a = key[r], b = key[r | J];
-                  const unsigned lo = a < b ? a : b, hi = a < b ? b : a;
-                  key[r] = asc ? lo : hi;
-                  key[r | J] = asc ? hi : lo;
-                }
-            }
-        } else {
-          // distance j >= E: the partner of slot t*E + r is slot (t ^ j/E)*E + r
-          const int tj = j / E;
-          const bool keep_min = ((t & tj) == 0) == (((t * E) & k) == 0);
-          if (tj < 32) {
-#pragma unroll
-            for (int r = 0; r < E; ++r) {
-              const unsigned o = __shfl_xor_sync(0xFFFFFFFFu, key[r], tj);
-              key[r] = keep_min ? (o < key[r] ? o : key[r]) : (o > key[r] ? o : key[r]);
-            }
-          } else {
-            __syncthreads();  // (the previous exchange's reads are done)
-#pragma unroll
-            for (int r = 0; r < E; ++r) s_key[t * E + r] = key[r];
-            __syncthreads();
-            const unsigned *src = s_key + (t ^ tj) * E;
-#pragma unroll
-            for (int r = 0; r < E; ++r) {
-              const unsigned o = src[r];
-              key[r] = keep_min ? (o < key[r] ? o : key[r]) : (o > key[r] ? o : key[r]);
-            }
-          }
-        }
+      const int e = r * NT + t;
+      if (e < v.stride) {
+        const unsigned ti = (unsigned)ri[e];
+        key[r] = ((ti < n ? ti : n) << pb) | (unsigned)e;
+        s_w[e] = rw[e];
       }
+    }
+    __syncthreads();
+    unsigned rank[E];
+#pragma unroll
+    for (int r = 0; r < E; ++r)
+      if (r * NT + t < v.stride) rank[r] = atomicAdd(s_cnt + ((key[r] >> pb) >> sh), 1u);
+    __syncthreads();
+    // exclusive scan of the counts: thread t's buckets t*per .. t*per+per-1, then warps
+    unsigned mine = 0;
+    for (int q = 0; q < per; ++q) mine += s_cnt[t * per + q];
+    unsigned incl = mine;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const unsigned o = __shfl_up_sync(0xFFFFFFFFu, incl, d);
+      if (lane >= d) incl += o;
+    }
+    if (lane == 31) s_part[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+      const int nw = NT >> 5;
+      unsigned x = lane < nw ? s_part[lane] : 0u, xi = x;
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        const unsigned o = __shfl_up_sync(0xFFFFFFFFu, xi, d);
+        if (lane >= d) xi += o;
+      }
+      if (lane < nw) s_part[lane] = xi - x;
+    }
+    __syncthreads();
+    unsigned start = s_part[warp] + incl - mine;
+    for (int q = 0; q < per; ++q) {
+      const unsigned c = s_cnt[t * per + q];
+      s_cnt[t * per + q] = start;
+      start += c;
+    }
     __syncthreads();
 #pragma unroll
-    for (int r = 0; r < E; ++r) s_key[t * E + r] = key[r];
+    for (int r = 0; r < E; ++r)
+      if (r * NT + t < v.stride) s_key[s_cnt[(key[r] >> pb) >> sh] + rank[r]] = key[r];
+    __syncthreads();
+    for (int b = t; b < nb; b += NT) {
+      const unsigned lo = s_cnt[b], hi = b + 1 < nb ? s_cnt[b + 1] : (unsigned)v.stride;
+      for (unsigned i = lo + 1; i < hi; ++i) {
+        const unsigned x = s_key[i];
+        unsigned j = i;
+        while (j > lo && s_key[j - 1] > x) {
+          s_key[j] = s_key[j - 1];
+          --j;
+        }
+        s_key[j] = x;
+      }
+    }
     __syncthreads();
     for (int e = t; e < v.stride; e += NT) {
-      const unsigned from = s_key[e] & smask;  // (the first stride keys are the row's own)
-      ri[e] = s_i[from];
-      rw[e] = s_w[from];
+      const unsigned k = s_key[e];
+      ri[e] = k < lim ? (int)(k >> pb) : -1;
+      rw[e] = s_w[k & smask];
     }
-    __syncthreads();  // (before the next row overwrites the shared copy)
+    __syncthreads();  // (before the next row overwrites the shared arrays)
   }
 }
 
@@ -1031,12 +1043,14 @@ static cudaError_t sort_rows_e(const NetView &v, int p2, int nt, cudaStream_t s)
 
 template <int E>
 static cudaError_t sort_gen_e(const NetView &v, int p2, int pb, cudaStream_t s) {
-  const int nt = p2 / E;
-  const size_t smem = (size_t)p2 * 4 + (size_t)v.stride * 8;
+  const int nt = p2 / E, nb = std::max(nt, p2 / 2);
+  int sh = 0;
+  while ((v.n >> sh) >= nb) ++sh;
+  const size_t smem = ((size_t)nb + 32 + 2 * (size_t)v.stride) * 4;
   unsigned g = 0;
   cudaError_t e = row_grid(k_sort_gen<E>, nt, smem, v.n, &g);
   if (e != cudaSuccess) return e;
-  k_sort_gen<E><<<g, nt, smem, s>>>(v, p2, pb);
+  k_sort_gen<E><<<g, nt, smem, s>>>(v, pb, nb, sh);
   return cudaGetLastError();
 }
 
@@ -1045,7 +1059,7 @@ cudaError_t launch_sort_rows(const NetView &v, bool generated, cudaStream_t s) {
   while (p2 < v.stride) p2 <<= 1, ++pb;
   if ((size_t)p2 * 8 > 200 * 1024) return cudaErrorInvalidValue;
   if (generated && ((uint64_t)v.n << pb) + (uint64_t)p2 - 1 < 0xFFFFFFFFull) {
-    // E consecutive keys a thread: 8 (up to 16 for rows longer than 8192), fewer for short rows
+    // E keys a thread: 8 (16 for rows longer than 8192), fewer for rows shorter than 256
     const int E = p2 / 32 < 8 ? p2 / 32 : (p2 / 8 > 1024 ? 16 : 8);
     switch (E) {
       case 1: return sort_gen_e<1>(v, p2, pb, s);
