@@ -58,12 +58,19 @@ struct TeamLaunch {
   int2 *d_slots = nullptr, *h_slots = nullptr;
   int *d_ctl = nullptr, *h_ctl = nullptr;  // [0] slot count, [1] queue head
   int *h_status = nullptr;                 // per item: status word, team error word
+  int64_t *d_off = nullptr, *h_off = nullptr;  // per item: its share of the pack (many networks)
+  unsigned char *d_pack = nullptr, *h_pack = nullptr;
+  size_t cap_pack = 0;
   int cap_items = 0, cap_slots = 0;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   // the round as a CUDA graph, replayed while its shape (networks, teams, buffers) holds
   cudaGraphExec_t exec = nullptr;
   std::vector<uint64_t> sig;
   std::vector<int> order;  // networks of the round in flight (team_round_start .. finish)
+  // a round of many networks, launched directly: its networks and steps, read back by pack
+  bool direct = false;
+  std::vector<g4s_net *> nets;
+  std::vector<int> steps;
   TeamLaunch() = default;
   TeamLaunch(const TeamLaunch &) = delete;
   TeamLaunch &operator=(const TeamLaunch &) = delete;
@@ -82,15 +89,23 @@ struct TeamLaunch {
     cudaFreeHost(h_slots);
     cudaFreeHost(h_ctl);
     cudaFreeHost(h_status);
+    cudaFree(d_off);
+    cudaFreeHost(h_off);
+    cudaFree(d_pack);
+    cudaFreeHost(h_pack);
     if (e0) cudaEventDestroy(e0);
     if (e1) cudaEventDestroy(e1);
     d_items = h_items = nullptr;
     d_slots = h_slots = nullptr;
     d_ctl = h_ctl = nullptr;
     h_status = nullptr;
+    d_off = h_off = nullptr;
+    d_pack = h_pack = nullptr;
+    cap_pack = 0;
     cap_items = cap_slots = 0;
     e0 = e1 = nullptr;
     order.clear();
+    direct = false;
   }
   int reserve(int items, int slots) {
     if (!e0 && (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess))
@@ -102,12 +117,17 @@ struct TeamLaunch {
       cudaFree(d_items);
       cudaFreeHost(h_items);
       cudaFreeHost(h_status);
+      cudaFree(d_off);
+      cudaFreeHost(h_off);
       d_items = h_items = nullptr;
       h_status = nullptr;
+      d_off = h_off = nullptr;
       cap_items = 0;  // (until the new buffers exist)
       if (cudaMalloc((void **)&d_items, sizeof(TeamItem) * items) != cudaSuccess ||
           cudaMallocHost((void **)&h_items, sizeof(TeamItem) * items) != cudaSuccess ||
-          cudaMallocHost((void **)&h_status, sizeof(int) * 2 * items) != cudaSuccess)
+          cudaMallocHost((void **)&h_status, sizeof(int) * 2 * items) != cudaSuccess ||
+          cudaMalloc((void **)&d_off, sizeof(int64_t) * items) != cudaSuccess ||
+          cudaMallocHost((void **)&h_off, sizeof(int64_t) * items) != cudaSuccess)
         return set_error(G4S_ERR_NOMEM, "team items");
       cap_items = items;
     }
@@ -122,6 +142,18 @@ struct TeamLaunch {
         return set_error(G4S_ERR_NOMEM, "team slots");
       cap_slots = slots;
     }
+    return G4S_OK;
+  }
+  int reserve_pack(size_t bytes) {
+    if (bytes <= cap_pack) return G4S_OK;
+    bytes = std::max(bytes, 2 * cap_pack);
+    cudaFree(d_pack);
+    cudaFreeHost(h_pack);
+    d_pack = h_pack = nullptr;
+    cap_pack = 0;
+    if (cudaMalloc((void **)&d_pack, bytes) != cudaSuccess || cudaMallocHost((void **)&h_pack, bytes) != cudaSuccess)
+      return set_error(G4S_ERR_NOMEM, "team round read-back buffer");
+    cap_pack = bytes;
     return G4S_OK;
   }
 };
@@ -824,6 +856,34 @@ static int team_round_start(g4s_net *const *nets, const int *steps, const bool *
     if (steps[i] <= 0) L.h_items[i].steps = 0;
   L.h_ctl[0] = nslots;
   L.h_ctl[1] = 0;
+  L.direct = count > 1;
+  if (L.direct) {
+    // Many networks: the set changes from round to round (a server admits and retires
+    // requests), so a graph would be captured and instantiated for almost every round, at a
+    // cost that grows with the networks.  Launched directly instead, in a fixed number of
+    // calls: descriptors up, one kernel clearing every network's per-launch words, the team
+    // kernel between two events, one kernel packing every network's results, one copy down.
+    size_t total = 0;
+    for (int i : order) {
+      L.h_off[i] = (int64_t)total;
+      total += round_pack_bytes(steps[i]);
+    }
+    if ((rc = L.reserve_pack(total))) return rc;
+    L.nets.assign(nets, nets + count);
+    L.steps.assign(steps, steps + count);
+    G4S_CUDA(cudaMemcpyAsync(L.d_items, L.h_items, sizeof(TeamItem) * count, cudaMemcpyHostToDevice, s));
+    G4S_CUDA(cudaMemcpyAsync(L.d_slots, L.h_slots, sizeof(int2) * nslots, cudaMemcpyHostToDevice, s));
+    G4S_CUDA(cudaMemcpyAsync(L.d_ctl, L.h_ctl, 8, cudaMemcpyHostToDevice, s));
+    G4S_CUDA(cudaMemcpyAsync(L.d_off, L.h_off, sizeof(int64_t) * count, cudaMemcpyHostToDevice, s));
+    G4S_CUDA(launch_round_clear(L.d_items, count, s));
+    G4S_CUDA(cudaEventRecord(L.e0, s));
+    G4S_CUDA(launch_team(L.d_items, L.d_slots, L.d_ctl, L.d_ctl + 1, grid, smem, limit_ns, stall, s, pair, nt));
+    G4S_CUDA(cudaEventRecord(L.e1, s));
+    G4S_CUDA(launch_round_gather(L.d_items, L.d_off, count, L.d_pack, s));
+    G4S_CUDA(cudaMemcpyAsync(L.h_pack, L.d_pack, total, cudaMemcpyDeviceToHost, s));
+    L.order = order;
+    return G4S_OK;
+  }
   // The round's graph: clear the networks' per-chunk arrays, error words and spike records,
   // upload the descriptors, the persistent launch between two timing events, and copy
   // back each network's per-step counts, offsets and stamps and its status words.  Its
@@ -895,6 +955,16 @@ static int team_round_finish(TeamLaunch &L, cudaStream_t s, double *kernel_ms, i
   G4S_CUDA(cudaEventElapsedTime(&ms, L.e0, L.e1));
   *kernel_ms += ms;
   *launches += 1;
+  if (L.direct)  // each network's share of the pack into its own pinned per-step buffers
+    for (int i : L.order) {
+      g4s_net *n = L.nets[(size_t)i];
+      const size_t st = (size_t)L.steps[(size_t)i];
+      const unsigned char *p = L.h_pack + L.h_off[i];
+      std::memcpy(L.h_status + 2 * i, p, 8);
+      std::memcpy(n->h_counts, p + 8, st * 4);
+      std::memcpy(n->h_base, p + 8 + ((st * 4 + 7) & ~(size_t)7), st * 8);
+      std::memcpy(n->h_stamps, p + 8 + ((st * 4 + 7) & ~(size_t)7) + st * 8, st * 16);
+    }
   for (int i : L.order) {
     const int rc = status_rc(L.h_status[2 * i], L.h_status[2 * i + 1], "team step kernel");
     if (rc) return rc;

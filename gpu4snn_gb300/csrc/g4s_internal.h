@@ -135,6 +135,13 @@ inline int team_window(int64_t rc, int team) {
 cudaError_t launch_sort_rows(const NetView &v, bool generated, cudaStream_t s);
 // *unsorted <- 1 if some row is not in launch_sort_rows' order, else 0
 cudaError_t launch_rows_sorted(const NetView &v, int *unsorted, cudaStream_t s);
+// A launch over many networks: clear (before it) and pack (after it) every network's
+// per-launch words; network i's share of the pack is round_pack_bytes(steps_i) bytes at
+// off[i]: status word, team error word, counts, raster offsets, stamps.
+inline size_t round_pack_bytes(int steps) { return 8 + (((size_t)steps * 4 + 7) & ~(size_t)7) + (size_t)steps * 24; }
+cudaError_t launch_round_clear(const TeamItem *items, int count, cudaStream_t s);
+cudaError_t launch_round_gather(const TeamItem *items, const int64_t *off, int count, unsigned char *pack,
+                                cudaStream_t s);
 cudaError_t launch_segoff(const NetView &v, int team, int64_t rc, uint16_t *seg, cudaStream_t s);
 cudaError_t launch_inbound(const NetView &v, unsigned *cnt, unsigned long long *mag, unsigned long long *out,
                            cudaStream_t s);

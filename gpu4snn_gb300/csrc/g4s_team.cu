@@ -1081,6 +1081,55 @@ cudaError_t launch_sort_rows(const NetView &v, bool generated, cudaStream_t s) {
   }
 }
 
+// ---------------------------------------------------------------------------------------
+// Set-up and read-back of a launch over many networks, one CTA per network.  k_round_clear
+// zeroes each network's per-step counts and stamps of the launch, its status word and its
+// team's error word and spike records; k_round_gather packs its status words, counts,
+// raster offsets and stamps at its offset in one buffer (round_pack_bytes each), which one
+// copy brings to the host.  Networks with no steps in the launch are skipped.
+// ---------------------------------------------------------------------------------------
+__global__ void k_round_clear(const TeamItem *items) {
+  const TeamItem &it = items[blockIdx.x];
+  const int s = it.steps;
+  if (s <= 0) return;
+  for (int i = threadIdx.x; i < s; i += blockDim.x) it.v.counts[i] = 0;
+  for (int i = threadIdx.x; i < 2 * s + 2; i += blockDim.x) it.v.stamps[i] = 0ull;
+  if (threadIdx.x == 0) *it.v.status = 0;
+  unsigned long long *g = reinterpret_cast<unsigned long long *>(it.sync);
+  const int64_t words = (int64_t)(1 + 2 * it.team * kRecLines) * (int64_t)(sizeof(GridSync) / 8);
+  for (int64_t i = threadIdx.x; i < words; i += blockDim.x) g[i] = 0ull;
+}
+
+__global__ void k_round_gather(const TeamItem *items, const int64_t *off, unsigned char *pack) {
+  const TeamItem &it = items[blockIdx.x];
+  const int s = it.steps;
+  if (s <= 0) return;
+  unsigned char *p = pack + off[blockIdx.x];
+  if (threadIdx.x == 0) {
+    reinterpret_cast<int *>(p)[0] = *it.v.status;
+    reinterpret_cast<int *>(p)[1] = it.sync->error;
+  }
+  int *c = reinterpret_cast<int *>(p + 8);
+  long long *b = reinterpret_cast<long long *>(p + 8 + (((size_t)s * 4 + 7) & ~(size_t)7));
+  unsigned long long *t = reinterpret_cast<unsigned long long *>(b + s);
+  for (int i = threadIdx.x; i < s; i += blockDim.x) {
+    c[i] = it.v.counts[i];
+    b[i] = it.v.base[i];
+  }
+  for (int i = threadIdx.x; i < 2 * s; i += blockDim.x) t[i] = it.v.stamps[i];
+}
+
+cudaError_t launch_round_clear(const TeamItem *items, int count, cudaStream_t s) {
+  k_round_clear<<<(unsigned)count, 256, 0, s>>>(items);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_round_gather(const TeamItem *items, const int64_t *off, int count, unsigned char *pack,
+                                cudaStream_t s) {
+  k_round_gather<<<(unsigned)count, 256, 0, s>>>(items, off, pack);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_segoff(const NetView &v, int team, int64_t rc, uint16_t *seg, cudaStream_t s) {
   int dev = 0, sms = 1;
   cudaGetDevice(&dev);
