@@ -343,7 +343,7 @@ def main():
     ap.add_argument("--no-schemes", action="store_true", help="skip timing the five schemes one by one")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-ensemble leg")
     ap.add_argument("--batch-networks", type=int, default=256, help="networks of the batched ensemble")
-    ap.add_argument("--served", default="200",
+    ap.add_argument("--served", default="50,200,1000",
                     help="comma-separated Poisson arrival rates (req/s) for the served leg ('' skips it)")
     ap.add_argument("--served-requests", type=int, default=200, help="requests per arrival rate")
     a = ap.parse_args()
