@@ -215,6 +215,7 @@ struct g4s_net {
   int64_t team_rc = 0;
   bool team_ready = false;
   bool team_batch = false;  // geometry planned for a multi-network batch
+  int64_t team_slice = 0;   // ... with this many neurons per CTA
   bool team_ok = true;
   bool pair_ready = false;  // the interleaved rows match the tables
   unsigned long long *list = nullptr;
@@ -557,7 +558,7 @@ static int resolve_alg(g4s_net *n, int alg) {
 // Returns false if the network does not fit or its tables break the exactness bound of
 // the split accumulation (the global-atomic persistent kernel is used instead).
 // ---------------------------------------------------------------------------------------
-static bool plan_team(g4s_net *n, int want, bool batch, int *p_out, int64_t *rc_out) {
+static bool plan_team(g4s_net *n, int want, bool batch, int64_t slice, int *p_out, int64_t *rc_out) {
   const NetView &v = n->v;
   if (!n->tables_fit) return false;
   int pmax = 0;
@@ -568,8 +569,9 @@ static bool plan_team(g4s_net *n, int want, bool batch, int *p_out, int64_t *rc_
   }
   pmax = std::min(pmax, kMaxTeam);
   // alone, a network spreads over the GPU (one CTA per 128 neurons, up to one per SM); in a
-  // batch it takes one CTA per 8192 neurons, so that more networks run at once
-  int64_t p = want > 0 ? want : (batch ? (v.n + kBatchSlice - 1) / kBatchSlice : (v.n + kSoloSlice - 1) / kSoloSlice);
+  // batch it takes one CTA per `slice` neurons (8192 unless the batch is small), so that more
+  // networks run at once
+  int64_t p = want > 0 ? want : (batch ? (v.n + slice - 1) / slice : (v.n + kSoloSlice - 1) / kSoloSlice);
   if (p < 1) p = 1;
   if (p > pmax) p = pmax;
   int64_t rc = (v.n + p - 1) / p;
@@ -590,12 +592,13 @@ static bool plan_team(g4s_net *n, int want, bool batch, int *p_out, int64_t *rc_
 
 // Team geometry, the per-step spike lists and, for teams of more than one CTA, the
 // per-row segment table.
-static int prepare_team(g4s_net *n, bool batch = false) {
-  if (n->team_ready && n->team_batch == batch) return G4S_OK;
+static int prepare_team(g4s_net *n, bool batch = false, int64_t slice = kBatchSlice) {
+  if (n->team_ready && n->team_batch == batch && (!batch || n->team_slice == slice)) return G4S_OK;
   int p = 0;
   int64_t rc = 0;
   n->team_batch = batch;
-  if (!plan_team(n, n->want_p, batch, &p, &rc)) {
+  n->team_slice = slice;
+  if (!plan_team(n, n->want_p, batch, slice, &p, &rc)) {
     n->team_ok = false;
     return G4S_OK;
   }
@@ -1131,14 +1134,36 @@ static int run_net(g4s_net *n, int32_t steps, int32_t alg_in) {
 // in one persistent launch.
 static int run_nets(g4s_net *const *nets, const int32_t *steps, int count, double *dev_ms, int64_t *launches) {
   if (count <= 0) return set_error(G4S_ERR_INVALID, "count must be > 0");
+  for (int i = 0; i < count; ++i)
+    if (!nets[i]) return set_error(G4S_ERR_INVALID, "null handle in batch");
+  // Neurons per CTA of the batch: kBatchSlice, unless the teams that gives leave SMs idle
+  // (few networks, as at a server's start and end): then the smallest power-of-two slice,
+  // down to a lone network's, whose teams still fit one CTA per SM together.  (Powers of
+  // two, so that a network's team, and its segment table, change only when the batch
+  // changes by a factor.)
+  int64_t slice = kBatchSlice;
+  if (count > 1) {
+    int gmax = 0;
+    if (team_max_blocks(kTeamSmemLimit, &gmax) != cudaSuccess || gmax < 1) {
+      (void)cudaGetLastError();
+      gmax = 0;
+    }
+    const int64_t pcap = std::min(gmax, kMaxTeam);
+    auto slots = [&](int64_t sl) {
+      int64_t t = 0;
+      for (int i = 0; i < count; ++i)
+        if (steps[i] > 0) t += std::min(pcap, (nets[i]->v.n + sl - 1) / sl);
+      return t;
+    };
+    while (gmax > 0 && slice > kSoloSlice && slots(slice / 2) <= gmax) slice /= 2;
+  }
   std::vector<int64_t> remaining(count);
   for (int i = 0; i < count; ++i) {
-    if (!nets[i]) return set_error(G4S_ERR_INVALID, "null handle in batch");
     if (steps[i] < 0 || nets[i]->t_abs + steps[i] > (int64_t)INT32_MAX)
       return set_error(G4S_ERR_INVALID, "bad step count in batch");
     for (int j = 0; j < i; ++j)
       if (nets[j] == nets[i]) return set_error(G4S_ERR_INVALID, "a handle appears twice in the batch");
-    int rc = prepare_team(nets[i], count > 1);
+    int rc = prepare_team(nets[i], count > 1, slice);
     if (rc) return rc;
     if (!nets[i]->team_ok)
       return set_error(G4S_ERR_INVALID, "a network of the batch does not fit the team kernel");
