@@ -1137,10 +1137,11 @@ static int run_nets(g4s_net *const *nets, const int32_t *steps, int count, doubl
   for (int i = 0; i < count; ++i)
     if (!nets[i]) return set_error(G4S_ERR_INVALID, "null handle in batch");
   // Neurons per CTA of the batch: kBatchSlice, unless the teams that gives leave SMs idle
-  // (few networks, as at a server's start and end): then the smallest power-of-two slice,
-  // down to a lone network's, whose teams still fit one CTA per SM together.  (Powers of
-  // two, so that a network's team, and its segment table, change only when the batch
-  // changes by a factor.)
+  // (few networks, as at a server's start and end): then the smallest slice of a fixed
+  // ladder (half octaves down to a lone network's), whose teams still fit one CTA per SM
+  // together.  (A ladder, so that a network's team, and its segment table, change only when
+  // the batch changes by a factor.)
+  static const int64_t kSlices[] = {kBatchSlice, 6144, 4096, 3072, 2048, 1536, 1024, 768, 512, 384, 256, 192, kSoloSlice};
   int64_t slice = kBatchSlice;
   if (count > 1) {
     int gmax = 0;
@@ -1155,7 +1156,8 @@ static int run_nets(g4s_net *const *nets, const int32_t *steps, int count, doubl
         if (steps[i] > 0) t += std::min(pcap, (nets[i]->v.n + sl - 1) / sl);
       return t;
     };
-    while (gmax > 0 && slice > kSoloSlice && slots(slice / 2) <= gmax) slice /= 2;
+    for (size_t k = 1; gmax > 0 && k < sizeof(kSlices) / sizeof(kSlices[0]) && slots(kSlices[k]) <= gmax; ++k)
+      slice = kSlices[k];
   }
   std::vector<int64_t> remaining(count);
   for (int i = 0; i < count; ++i) {
