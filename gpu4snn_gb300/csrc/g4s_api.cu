@@ -664,28 +664,32 @@ static int prepare_team(g4s_net *n, bool batch = false, int64_t slice = kBatchSl
 // into any neuron and sum(|q| >> 16) + 1 over them below 2^31 - 2^20.
 static int finish_tables(g4s_net *n, bool may_be_sorted) {
   // (rows that arrive sorted, as tables read back from a network do, skip the sort)
+  // Scratch is stream-ordered (cudaMallocAsync / cudaFreeAsync on the network's stream):
+  // a plain cudaFree waits for the whole device, i.e. for whatever other networks are
+  // running, where a server creates networks while its rounds run.
+  cudaStream_t st = n->stream;
   int *flag = nullptr, h_unsorted = 1;
-  cudaError_t ef = may_be_sorted ? cudaMalloc((void **)&flag, sizeof(int)) : cudaSuccess;
-  if (ef == cudaSuccess && flag) ef = launch_rows_sorted(n->v, flag, n->stream);
-  if (ef == cudaSuccess && flag) ef = cudaMemcpyAsync(&h_unsorted, flag, sizeof(int), cudaMemcpyDeviceToHost, n->stream);
-  if (ef == cudaSuccess && flag) ef = cudaStreamSynchronize(n->stream);
-  cudaFree(flag);
+  cudaError_t ef = may_be_sorted ? cudaMallocAsync((void **)&flag, sizeof(int), st) : cudaSuccess;
+  if (ef == cudaSuccess && flag) ef = launch_rows_sorted(n->v, flag, st);
+  if (ef == cudaSuccess && flag) ef = cudaMemcpyAsync(&h_unsorted, flag, sizeof(int), cudaMemcpyDeviceToHost, st);
+  if (flag) cudaFreeAsync(flag, st);
+  if (ef == cudaSuccess && flag) ef = cudaStreamSynchronize(st);
   if (ef != cudaSuccess) return cuda_error(ef, "row order check");
-  if (h_unsorted) G4S_CUDA(launch_sort_rows(n->v, !may_be_sorted, n->stream));
+  if (h_unsorted) G4S_CUDA(launch_sort_rows(n->v, !may_be_sorted, st));
   n->team_ready = false;
   n->pair_ready = false;
   unsigned *cnt = nullptr;
   unsigned long long *mag = nullptr, *out = nullptr;
-  cudaError_t e = cudaMalloc((void **)&cnt, (size_t)n->v.n * 4);
-  if (e == cudaSuccess) e = cudaMalloc((void **)&mag, (size_t)n->v.n * 8);
-  if (e == cudaSuccess) e = cudaMalloc((void **)&out, 16);
+  cudaError_t e = cudaMallocAsync((void **)&cnt, (size_t)n->v.n * 4, st);
+  if (e == cudaSuccess) e = cudaMallocAsync((void **)&mag, (size_t)n->v.n * 8, st);
+  if (e == cudaSuccess) e = cudaMallocAsync((void **)&out, 16, st);
   unsigned long long h[2] = {~0ull, ~0ull};
-  if (e == cudaSuccess) e = launch_inbound(n->v, cnt, mag, out, n->stream);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(h, out, 16, cudaMemcpyDeviceToHost, n->stream);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(n->stream);
-  cudaFree(cnt);
-  cudaFree(mag);
-  cudaFree(out);
+  if (e == cudaSuccess) e = launch_inbound(n->v, cnt, mag, out, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(h, out, 16, cudaMemcpyDeviceToHost, st);
+  if (cnt) cudaFreeAsync(cnt, st);
+  if (mag) cudaFreeAsync(mag, st);
+  if (out) cudaFreeAsync(out, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return cuda_error(e, "table bound pass");
   n->max_in = h[0];
   n->max_mag = h[1];
