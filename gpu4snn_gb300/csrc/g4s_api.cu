@@ -439,6 +439,8 @@ static int reset_net(g4s_net *n) {
   return G4S_OK;
 }
 
+static int prepare_rows(g4s_net *n);  // (defined with the team set-up below)
+
 // ---------------------------------------------------------------------------------------
 // Host generator of the reference's tables (glibc rand).  The k-th remaining target of a
 // row is found by a binary search over the sorted list of targets already taken, which
@@ -483,6 +485,8 @@ int conn_glibc_host(unsigned seed, int32_t n, int32_t nsyn, int32_t stride, int3
   }
   return G4S_OK;
 }
+
+int net_prepare_rows(g4s_net *n) { return n && n->tables_fit ? prepare_rows(n) : G4S_OK; }
 
 double net_recent_step_ms(const g4s_net *n, int64_t k) {
   double sum = 0.0;
@@ -590,6 +594,37 @@ static bool plan_team(g4s_net *n, int want, bool batch, int64_t slice, int *p_ou
   return true;
 }
 
+// The team kernel's buffers that do not depend on the team: the interleaved rows of its
+// segment reads (optional: without them, as when the device has no room left for them, the
+// kernel reads the separate arrays) and the tagged spike lists.  Both are ready on return
+// (a batch may launch on another handle's stream).
+static int prepare_rows(g4s_net *n) {
+  if (!n->v.pair) {
+    const size_t bytes = (size_t)n->v.n * (size_t)n->v.stride * sizeof(int2);
+    if (!g_fail_next_alloc.exchange(0) && cudaMalloc((void **)&n->v.pair, bytes) == cudaSuccess) {
+      n->device_bytes += bytes;
+      n->pair_ready = false;
+    } else {
+      (void)cudaGetLastError();
+      n->v.pair = nullptr;
+    }
+  }
+  if (n->v.pair && !n->pair_ready) {
+    G4S_CUDA(launch_pairs(n->v, n->stream));
+    G4S_CUDA(cudaStreamSynchronize(n->stream));
+    n->pair_ready = true;
+  }
+  if (!n->list) {
+    cudaError_t e = cudaMalloc((void **)&n->list, (size_t)n->v.n * 4 * sizeof(unsigned long long));
+    if (e != cudaSuccess) return cuda_error(e, "spike lists");
+    G4S_CUDA(cudaMemsetAsync(n->list, 0, (size_t)n->v.n * 4 * sizeof(unsigned long long), n->stream));
+    G4S_CUDA(cudaStreamSynchronize(n->stream));
+    n->tag_next = 0;
+    n->device_bytes += (size_t)n->v.n * 4 * sizeof(unsigned long long);
+  }
+  return G4S_OK;
+}
+
 // Team geometry, the per-step spike lists and, for teams of more than one CTA, the
 // per-row segment table.
 static int prepare_team(g4s_net *n, bool batch = false, int64_t slice = kBatchSlice) {
@@ -612,30 +647,8 @@ static int prepare_team(g4s_net *n, bool batch = false, int64_t slice = kBatchSl
     const double syn = (double)n->v.n * recent_rate(n) / 1000.0 * (double)n->v.nsyn / (double)p;
     n->team_nt_eff = !batch && syn < 32768.0 ? kTeamNTSmall : kTeamNT;
   }
-  // the interleaved rows of the team kernel's segment reads: optional (without them, as
-  // when the device has no room left for them, the kernel reads the separate arrays)
-  if (!n->v.pair) {
-    const size_t bytes = (size_t)n->v.n * (size_t)n->v.stride * sizeof(int2);
-    if (!g_fail_next_alloc.exchange(0) && cudaMalloc((void **)&n->v.pair, bytes) == cudaSuccess) {
-      n->device_bytes += bytes;
-      n->pair_ready = false;
-    } else {
-      (void)cudaGetLastError();
-      n->v.pair = nullptr;
-    }
-  }
-  if (n->v.pair && !n->pair_ready) {
-    G4S_CUDA(launch_pairs(n->v, n->stream));
-    n->pair_ready = true;
-  }
-  if (!n->list) {
-    cudaError_t e = cudaMalloc((void **)&n->list, (size_t)n->v.n * 4 * sizeof(unsigned long long));
-    if (e != cudaSuccess) return cuda_error(e, "spike lists");
-    G4S_CUDA(cudaMemsetAsync(n->list, 0, (size_t)n->v.n * 4 * sizeof(unsigned long long), n->stream));
-    G4S_CUDA(cudaStreamSynchronize(n->stream));  // a batch may launch on another handle's stream
-    n->tag_next = 0;
-    n->device_bytes += (size_t)n->v.n * 4 * sizeof(unsigned long long);
-  }
+  int rc0 = prepare_rows(n);
+  if (rc0) return rc0;
   if (p > 1) {
     const size_t bytes = (size_t)n->v.n * (size_t)(p + 1) * sizeof(uint16_t);
     if (bytes > n->seg_bytes) {

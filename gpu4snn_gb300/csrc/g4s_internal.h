@@ -161,6 +161,9 @@ cudaError_t launch_pairs(const NetView &v, cudaStream_t s);
 cudaError_t team_max_blocks(size_t smem, int *out, int nt = kTeamNT);
 // mean duration in ms of the last k simulated steps of a handle with a step time (0: none)
 double net_recent_step_ms(const g4s_net *n, int64_t k);
+// the team kernel's team-independent buffers of a handle (its interleaved rows and spike
+// lists), made ready ahead of its first team run; nothing for tables the kernel cannot run
+int net_prepare_rows(g4s_net *n);
 cudaError_t team_smem_ceiling();  // the part of team_max_blocks that launch_team needs
 // shared memory of one rank of a team of `team` CTAs with `rc` neurons each (0: does not fit)
 size_t team_smem(int64_t rc, int team);

@@ -134,7 +134,12 @@ static void admit_loop(g4s_server *s) {
     d.drive_scale = r->req.drive_scale;
     d.record_raster = r->req.record_raster;
     d.raster_budget_bytes = r->req.record_raster ? 4 * r->req.n * (int64_t)s->quantum : 0;
-    const int rc = g4s_net_create(&d, &r->net);
+    int rc = g4s_net_create(&d, &r->net);
+    // (the team kernel's rows and lists here, off the round thread)
+    if (rc == 0 && (rc = net_prepare_rows(r->net)) != 0) {
+      g4s_net_destroy(r->net);
+      r->net = nullptr;
+    }
     r->t_admit = Clock::now();
     lk.lock();
     if (rc != 0) {
