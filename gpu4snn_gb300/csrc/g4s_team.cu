@@ -285,15 +285,18 @@ __global__ void k_pairs(NetView v, int2 *pair) {
 
 // Exactness bound of the split accumulation: per target, the number of incoming synapses
 // and the sum of (|q| >> 16) + 1 over them; out[0] = max count, out[1] = max sum.
+// (mag null: the in-degrees only)
 __global__ void k_inbound(NetView v, unsigned *cnt, unsigned long long *mag) {
   const int64_t total = v.n * (int64_t)v.stride;
   for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < total; g += (int64_t)gridDim.x * blockDim.x) {
     const int t = v.idx[g];
     if (t < 0) continue;
-    const long long q = wfix(v.w[g]);
-    const unsigned long long a = (unsigned long long)(q < 0 ? -q : q) >> 16;
     atomicAdd(cnt + t, 1u);
-    atomicAdd(mag + t, a + 1ull);
+    if (mag) {
+      const long long q = wfix(v.w[g]);
+      const unsigned long long a = (unsigned long long)(q < 0 ? -q : q) >> 16;
+      atomicAdd(mag + t, a + 1ull);
+    }
   }
 }
 
@@ -302,7 +305,7 @@ __global__ void k_inbound_max(int64_t n, const unsigned *cnt, const unsigned lon
   unsigned long long mc = 0, mm = 0;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     mc = max(mc, (unsigned long long)cnt[i]);
-    mm = max(mm, mag[i]);
+    if (mag) mm = max(mm, mag[i]);
   }
   atomicMax(out, mc);
   atomicMax(out + 1, mm);
@@ -1146,7 +1149,7 @@ cudaError_t launch_inbound(const NetView &v, unsigned *cnt, unsigned long long *
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaError_t e = cudaMemsetAsync(cnt, 0, (size_t)v.n * 4, s);
-  if (e == cudaSuccess) e = cudaMemsetAsync(mag, 0, (size_t)v.n * 8, s);
+  if (e == cudaSuccess && mag) e = cudaMemsetAsync(mag, 0, (size_t)v.n * 8, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(out, 0, 16, s);
   if (e != cudaSuccess) return e;
   k_inbound<<<(unsigned)(sms * 8), 512, 0, s>>>(v, cnt, mag);
