@@ -58,9 +58,11 @@ constexpr int64_t kRoundMaxSteps = 16384;
 int64_t estimate_bytes(const g4s_request &r, int32_t quantum) {
   const int64_t stride = ((int64_t)r.nsyn + 3) / 4 * 4;
   const int64_t raster = r.record_raster ? 4 * r.n * (int64_t)quantum : ((int64_t)64 << 20);
-  // tables (and their interleaved copy), neuron state and statistics, spike lists, raster,
-  // per-step arrays
-  return r.n * stride * 16 + r.n * (8 + 16 + 4 + 8 + 4 + 32 + 32 + 4) + raster + 16384 * 28 + ((int64_t)1 << 20);
+  // tables (and their interleaved copy), neuron state and statistics, spike lists, the
+  // segment table at the largest team (a small batch spreads a network over the GPU),
+  // raster, per-step arrays
+  return r.n * stride * 16 + r.n * (8 + 16 + 4 + 8 + 4 + 32 + 32 + 4) + r.n * (kMaxTeam + 1) * 2 + raster +
+         16384 * 28 + ((int64_t)1 << 20);
 }
 
 }  // namespace
