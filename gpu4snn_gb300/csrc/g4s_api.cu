@@ -788,15 +788,39 @@ static void chunk_finish_from(g4s_net *n, int cs, const int *counts, const long 
     const size_t off = n->rt.size();
     n->rt.resize(off + (size_t)total);
     n->rid.resize(off + (size_t)total);
-    for (int lt = 0; lt < cs; ++lt) {
-      int *b = n->h_raster + base[lt];
-      sort_step_ids(b, counts[lt]);
-      const int32_t t = (int32_t)(t0 + lt);
-      int32_t *rt = n->rt.data() + off + (size_t)base[lt], *rid = n->rid.data() + off + (size_t)base[lt];
-      for (int q = 0; q < counts[lt]; ++q) {
-        rt[q] = t;
-        rid[q] = b[q];
+    auto steps = [&](int l0, int l1) {
+      for (int lt = l0; lt < l1; ++lt) {
+        int *b = n->h_raster + base[lt];
+        sort_step_ids(b, counts[lt]);
+        const int32_t t = (int32_t)(t0 + lt);
+        int32_t *rt = n->rt.data() + off + (size_t)base[lt], *rid = n->rid.data() + off + (size_t)base[lt];
+        for (int q = 0; q < counts[lt]; ++q) {
+          rt[q] = t;
+          rid[q] = b[q];
+        }
       }
+    };
+    // a large chunk on several host threads, each a run of whole steps (steps are independent)
+    const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    const int parts = total >= ((int64_t)1 << 20) ? (int)std::min<int64_t>(hw, cs) : 1;
+    if (parts <= 1) {
+      steps(0, cs);
+    } else {
+      std::vector<std::thread> pool;
+      int l0 = 0;
+      for (int p = 0; p < parts; ++p) {
+        // the steps up to the p+1-th share of the chunk's ids
+        const int64_t goal = total * (p + 1) / parts;
+        int l1 = l0;
+        while (l1 < cs && (p == parts - 1 || (int64_t)base[l1] < goal)) ++l1;
+        if (p == parts - 1) {
+          steps(l0, l1);
+        } else if (l1 > l0) {
+          pool.emplace_back(steps, l0, l1);
+        }
+        l0 = l1;
+      }
+      for (auto &th : pool) th.join();
     }
   }
   for (int lt = 0; lt < cs; ++lt) {
@@ -1638,8 +1662,19 @@ int g4s_net_raster(g4s_net *n, int32_t *t, int32_t *id, int64_t cap, int64_t *si
   const int64_t m = std::min(s, cap);
   if (m > 0) {
     if (!t || !id) return set_error(G4S_ERR_INVALID, "null raster buffer");
-    memcpy(t, n->rt.data(), (size_t)m * 4);
-    memcpy(id, n->rid.data(), (size_t)m * 4);
+    // large rasters on several host threads (a fresh destination is mostly page faults)
+    const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    const int64_t parts = m >= ((int64_t)1 << 21) ? (int64_t)hw : 1, per = (m + parts - 1) / parts;
+    auto part = [&](int64_t p) {
+      const int64_t lo = p * per, hi = std::min(m, lo + per);
+      if (lo >= hi) return;
+      memcpy(t + lo, n->rt.data() + lo, (size_t)(hi - lo) * 4);
+      memcpy(id + lo, n->rid.data() + lo, (size_t)(hi - lo) * 4);
+    };
+    std::vector<std::thread> pool;
+    for (int64_t p = 1; p < parts; ++p) pool.emplace_back(part, p);
+    part(0);
+    for (auto &th : pool) th.join();
   }
   return G4S_OK;
 }

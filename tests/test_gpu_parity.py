@@ -126,6 +126,24 @@ def test_chunked_run_matches(g4s, oracle):
             compare_state(net, sim)
 
 
+def test_large_raster_matches_oracle(g4s, oracle):
+    """N=100,000 x 1000 for 4000 steps (about 2.8 million spikes): the host files chunks of
+    more than 2^20 ids on several threads and copies the raster out on several threads;
+    the raster, counts and state equal the oracle's."""
+    n, nsyn, seed, steps = 100_000, 1000, 2, 4000
+    d, (idx, w) = oracle_tables(oracle, n, nsyn, seed)
+    sim = oracle.Sim(d, idx, w)
+    sim.run(steps, threads=16)
+    with g4s.Network(n, nsyn, seed=seed) as net:
+        net.run(steps, 4)
+        t, i = net.raster()
+        assert len(t) > (1 << 21)
+        ot, oi = sim.raster()
+        assert np.array_equal(t, ot) and np.array_equal(i, oi)
+        assert np.array_equal(net.counts(), sim.counts())
+        compare_state(net, sim)
+
+
 @pytest.mark.parametrize("alg", [0, 1, 2, 3])
 def test_host_driven_chunk_graphs(g4s, oracle, alg):
     """The host-driven schemes run their 512-step chunks as CUDA graphs, replayed for every
