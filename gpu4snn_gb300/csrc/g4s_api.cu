@@ -675,17 +675,18 @@ static int prepare_team(g4s_net *n, bool batch = false, int64_t slice = kBatchSl
 // segment table of the team kernel is rebuilt on the next SKL run.  The exactness bound
 // of the split shared-memory accumulation is measured here: fewer than 65536 synapses
 // into any neuron and sum(|q| >> 16) + 1 over them below 2^31 - 2^20.
-// In-degree (h[0]) and, with with_mag, the largest sum(|q| >> 16) + 1 over a neuron's
-// inputs (h[1]) of the tables, on the network's stream (stream-ordered scratch).
-static int bound_pass(g4s_net *n, bool with_mag, unsigned long long h[2]) {
+// Largest in-degree (h[0]) of the tables and, with with_mag, the largest sum(|q| >> 16) + 1
+// over a neuron's inputs (h[1]), else the largest (|q| >> 16) + 1 of any synapse (h[2]); on
+// the network's stream (stream-ordered scratch).
+static int bound_pass(g4s_net *n, bool with_mag, unsigned long long h[3]) {
   cudaStream_t st = n->stream;
   unsigned *cnt = nullptr;
   unsigned long long *mag = nullptr, *out = nullptr;
   cudaError_t e = cudaMallocAsync((void **)&cnt, (size_t)n->v.n * 4, st);
   if (e == cudaSuccess && with_mag) e = cudaMallocAsync((void **)&mag, (size_t)n->v.n * 8, st);
-  if (e == cudaSuccess) e = cudaMallocAsync((void **)&out, 16, st);
+  if (e == cudaSuccess) e = cudaMallocAsync((void **)&out, 24, st);
   if (e == cudaSuccess) e = launch_inbound(n->v, cnt, mag, out, st);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(h, out, 16, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(h, out, 24, cudaMemcpyDeviceToHost, st);
   if (cnt) cudaFreeAsync(cnt, st);
   if (mag) cudaFreeAsync(mag, st);
   if (out) cudaFreeAsync(out, st);
@@ -709,22 +710,19 @@ static int finish_tables(g4s_net *n, bool may_be_sorted) {
   if (h_unsorted) G4S_CUDA(launch_sort_rows(n->v, !may_be_sorted, st));
   n->team_ready = false;
   n->pair_ready = false;
-  // The bound.  Generated rows need only the in-degrees: each of their weights has |w| <=
-  // 1000 / nsyn (the law's scale times a uniform below 1), so sum(|q| >> 16) + 1 over a
-  // neuron's inputs is at most its in-degree x (1000 / nsyn x 2^16 + 1) (+ a margin for
-  // the float scale's rounding), which settles the bound unless some in-degree is about
-  // 32 x nsyn; then, and for uploaded tables, the magnitudes are summed as well.
-  unsigned long long h[2] = {~0ull, ~0ull};
-  int rc = bound_pass(n, may_be_sorted, h);
+  // The bound.  One pass counts the in-degrees and finds the largest term (|q| >> 16) + 1
+  // of any synapse: sum(|q| >> 16) + 1 over a neuron's inputs is at most its in-degree x
+  // that term, which settles the bound unless some neuron has many large inputs (for the
+  // generated law, an in-degree of about 32 x nsyn); only then are the sums formed exactly,
+  // by a second pass with one more atomic per synapse.
+  unsigned long long h[3] = {~0ull, ~0ull, ~0ull};
+  int rc = bound_pass(n, false, h);
   if (rc) return rc;
-  if (!may_be_sorted) {
-    const double term = std::floor(1000.0 / (double)n->v.nsyn * 65536.0 * (1.0 + 1e-6)) + 2.0;
-    const double bound = (double)h[0] * term;
-    if (bound < (double)((1ull << 31) - (1ull << 20)))
-      h[1] = (unsigned long long)bound;  // (an upper bound of the sum)
-    else if ((rc = bound_pass(n, true, h)))
-      return rc;
-  }
+  const unsigned long long limit = (1ull << 31) - (1ull << 20);
+  if (h[0] < 65536ull && h[2] < limit && h[0] * h[2] < limit)
+    h[1] = h[0] * h[2];  // (an upper bound of the sum)
+  else if ((rc = bound_pass(n, true, h)))
+    return rc;
   n->max_in = h[0];
   n->max_mag = h[1];
   n->tables_fit = h[0] < 65536ull && h[1] < (1ull << 31) - (1ull << 20);

@@ -143,6 +143,8 @@ cudaError_t launch_round_clear(const TeamItem *items, int count, cudaStream_t s)
 cudaError_t launch_round_gather(const TeamItem *items, const int64_t *off, int count, unsigned char *pack,
                                 cudaStream_t s);
 cudaError_t launch_segoff(const NetView &v, int team, int64_t rc, uint16_t *seg, cudaStream_t s);
+// out (3 words): the largest in-degree, the largest sum(|q| >> 16) + 1 over a neuron's
+// inputs (with mag, n words of scratch; else 0), the largest (|q| >> 16) + 1 (without mag)
 cudaError_t launch_inbound(const NetView &v, unsigned *cnt, unsigned long long *mag, unsigned long long *out,
                            cudaStream_t s);
 // team_max_blocks also raises the kernel's shared-memory ceiling: call it once before the

@@ -285,18 +285,26 @@ __global__ void k_pairs(NetView v, int2 *pair) {
 
 // Exactness bound of the split accumulation: per target, the number of incoming synapses
 // and the sum of (|q| >> 16) + 1 over them; out[0] = max count, out[1] = max sum.
-// (mag null: the in-degrees only)
-__global__ void k_inbound(NetView v, unsigned *cnt, unsigned long long *mag) {
+// Per neuron the in-degree and, with mag, sum(|q| >> 16) + 1 over its inputs; without mag,
+// the largest (|q| >> 16) + 1 of the table into *term instead.
+__global__ void k_inbound(NetView v, unsigned *cnt, unsigned long long *mag, unsigned long long *term) {
   const int64_t total = v.n * (int64_t)v.stride;
+  unsigned long long mx = 0;
   for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < total; g += (int64_t)gridDim.x * blockDim.x) {
     const int t = v.idx[g];
     if (t < 0) continue;
     atomicAdd(cnt + t, 1u);
-    if (mag) {
-      const long long q = wfix(v.w[g]);
-      const unsigned long long a = (unsigned long long)(q < 0 ? -q : q) >> 16;
-      atomicAdd(mag + t, a + 1ull);
-    }
+    const long long q = wfix(v.w[g]);
+    const unsigned long long a = ((unsigned long long)(q < 0 ? -q : q) >> 16) + 1ull;
+    if (mag)
+      atomicAdd(mag + t, a);
+    else
+      mx = max(mx, a);
+  }
+  if (!mag) {
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) mx = max(mx, __shfl_xor_sync(0xFFFFFFFFu, mx, d));
+    if ((threadIdx.x & 31) == 0) atomicMax(term, mx);
   }
 }
 
@@ -1150,9 +1158,9 @@ cudaError_t launch_inbound(const NetView &v, unsigned *cnt, unsigned long long *
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaError_t e = cudaMemsetAsync(cnt, 0, (size_t)v.n * 4, s);
   if (e == cudaSuccess && mag) e = cudaMemsetAsync(mag, 0, (size_t)v.n * 8, s);
-  if (e == cudaSuccess) e = cudaMemsetAsync(out, 0, 16, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(out, 0, 24, s);
   if (e != cudaSuccess) return e;
-  k_inbound<<<(unsigned)(sms * 8), 512, 0, s>>>(v, cnt, mag);
+  k_inbound<<<(unsigned)(sms * 8), 512, 0, s>>>(v, cnt, mag, out + 2);
   k_inbound_max<<<(unsigned)(sms * 2), 512, 0, s>>>(v.n, cnt, mag, out);
   return cudaGetLastError();
 }
