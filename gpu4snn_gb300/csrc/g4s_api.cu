@@ -1528,18 +1528,27 @@ int g4s_net_load_tables(g4s_net *n, const int32_t *idx, const float *w, int32_t 
     return set_error(G4S_ERR_INVALID, "table stride must be " + std::to_string(v.stride));
   const size_t cnt = (size_t)v.n * (size_t)v.stride, bytes = cnt * 4;
   // every target must be a neuron of this network or negative (an unused slot): checked on
-  // all host cores, the first offending entry reported
+  // all host cores, block by block (the largest target of 4096, a loop the compiler
+  // vectorises; a block over the limit is searched for its first offending entry), the
+  // first offending entry of the table reported
   {
     const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
     const size_t parts = cnt >= ((size_t)1 << 22) ? hw : 1, per = (cnt + parts - 1) / parts;
+    const int32_t nn = (int32_t)v.n;  // (n < 2^31)
     std::vector<size_t> bad(parts, SIZE_MAX);
     auto scan = [&](size_t p) {
       const size_t end = std::min(cnt, (p + 1) * per);
-      for (size_t k = p * per; k < end; ++k)
-        if (idx[k] >= v.n) {
-          bad[p] = k;
-          return;
-        }
+      for (size_t k0 = p * per; k0 < end; k0 += 4096) {
+        const size_t k1 = std::min(end, k0 + 4096);
+        int32_t mx = INT32_MIN;
+        for (size_t k = k0; k < k1; ++k) mx = std::max(mx, idx[k]);
+        if (mx < nn) continue;
+        for (size_t k = k0; k < k1; ++k)
+          if (idx[k] >= nn) {
+            bad[p] = k;
+            return;
+          }
+      }
     };
     std::vector<std::thread> pool;
     for (size_t p = 1; p < parts; ++p) pool.emplace_back(scan, p);

@@ -254,6 +254,27 @@ def test_block_threads_automatic_choice(g4s):
         assert e.value.code == _lib.ERR_INVALID
 
 
+def test_upload_with_a_target_out_of_range(g4s, oracle):
+    """A target >= n anywhere in a large upload (validated in parallel, block by block) is
+    refused with its position, and the network keeps its tables: it still runs as before."""
+    from gpu4snn_gb300 import _lib
+    n, nsyn, seed = 20_000, 300, 12
+    d, (idx, w) = oracle_tables(oracle, n, nsyn, seed)
+    sim = oracle.Sim(d, idx, w)
+    sim.run(60, threads=8)
+    with g4s.Network(n, nsyn, seed=seed) as net:
+        for pos in (n * nsyn - 1, 3_000_001, 5):
+            bad = idx.copy()
+            bad.flat[pos] = n
+            bad.flat[n * nsyn - 2] = n + 7  # (a later offender: the first is reported)
+            with pytest.raises(g4s.G4SError) as e:
+                net.load_tables(bad, w)
+            assert e.value.code == _lib.ERR_INVALID
+            assert f"table entry {min(pos, n * nsyn - 2)} " in str(e.value)
+        net.run(60, 4)
+        assert np.array_equal(np.stack(net.raster()), np.stack(sim.raster()))
+
+
 def test_uploaded_tables_with_holes(g4s, oracle):
     """Caller tables may leave slots unused (negative target) anywhere in a row."""
     n, nsyn, seed = 3000, 200, 8
