@@ -197,7 +197,7 @@ int64_t g4o_wfix(float w) {
 static inline int64_t n_exc_of(const g4o_desc *d) { return (d->n * (int64_t)d->exc_permille) / 1000; }
 
 /* ---------------------------------------------------------------------------------
- * Connectivity, Philox law (this build's default).  Row i gets nsyn distinct targets
+ * Connectivity, Philox law (the library's default).  Row i gets nsyn distinct targets
  * uniformly from [0,n) (minus i unless self loops), in draw order: draw k is accepted
  * iff its target was not accepted before.  Weight of slot j: (1000/nsyn)*0.5*U for
  * excitatory rows, (1000/nsyn)*(-1)*U for inhibitory ones, U = 24-bit uniform of word

@@ -11,7 +11,7 @@
  *   - connectivity law and weights   gpu4snn.cu:862-899
  *   - N_exc = floor(4N/5)            gpu4snn.cu:744
  * The reference draws its randomness from cuRAND XORWOW (seeded with time(NULL)) and
- * glibc rand(); this build replaces both with a counter-based Philox4x64-10 stream
+ * glibc rand(); the library replaces both with a counter-based Philox4x64-10 stream
  * (Salmon et al., SC'11) whose layout is defined below, so that CPU and GPU produce
  * identical bits.  Currents are accumulated as Q32.32 fixed point, which makes the
  * result independent of the order of the additions.
