@@ -48,6 +48,36 @@ def test_server_results_same_alone_and_in_mix(g4s):
             srv.release(rid)
 
 
+def test_served_requests_against_the_oracle(g4s, oracle):
+    """Spot checks of served requests: each served raster equals the FP32 oracle's bit for
+    bit, and for sampled requests the firing rate and ISI CV are within 1% of the FP64
+    oracle's (the same random draws in double precision; 0.47% and 0.13% here: the runs are
+    chaotic, so the precisions' trajectories separate, but their statistics agree)."""
+    from gpu4snn_gb300.server import Server
+    specs = [(2500, 1000, 2000, 1, 1.0, True), (4000, 400, 2000, 9, 1.3, True), (3000, 600, 2000, 21, 0.8, False)]
+    with Server(hbm_budget_bytes=4 << 30, quantum=250) as srv:
+        ids = [srv.submit(n, s, st, seed, d, record_raster=True) for n, s, st, seed, d, _ in specs]
+        results = _wait_all(srv, len(specs))
+        assert len(results) == len(specs)
+        for rid, (n, s, st, seed, d, fp64) in zip(ids, specs):
+            r = results[rid]
+            assert r.status == 0 and r.steps_done == st
+            got = srv.result(rid)
+            desc = oracle.make_desc(n, s, seed, drive_scale=d)
+            idx, w = oracle.conn_philox(desc)
+            s32 = oracle.Sim(desc, idx, w, oracle.FP32)
+            s32.run(st, threads=8)
+            t, i = s32.raster()
+            assert np.array_equal(got["t"], t) and np.array_equal(got["id"], i), n
+            if fp64:
+                s64 = oracle.Sim(desc, idx, w, oracle.FP64)
+                s64.run(st)
+                ref = s64.stats()
+                assert abs(r.rate_hz - ref.rate_hz) / ref.rate_hz < 0.01
+                assert abs(r.isi_cv - ref.isi_cv) / ref.isi_cv < 0.01
+            srv.release(rid)
+
+
 def test_server_budget_and_rejections(g4s):
     from gpu4snn_gb300 import _lib
     from gpu4snn_gb300.server import Server
