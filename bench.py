@@ -334,6 +334,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="n100k")
+    ap.add_argument("--drive", type=float, default=None,
+                    help="drive scale in place of the workload's (0.5 quiet, 1 balanced, 1.5-2 irregular)")
     ap.add_argument("--algorithm", default="AUTO")
     ap.add_argument("--block-threads", type=int, default=0,
                     help="threads per CTA of the SKL team kernel, 1024 or 768 (0: default / autotuned)")
@@ -351,6 +353,9 @@ def main():
         a.warmup = 3
     ws, rank, local, pg = dist_setup()
     cfg = WORKLOADS[a.workload]
+    drive_override = a.drive is not None and a.drive != cfg[3]
+    if drive_override:
+        cfg = cfg[:3] + (float(a.drive),) + cfg[4:]
     if a.impl == "reference":
         return run_reference(a, cfg, ws, rank, pg)
 
@@ -417,7 +422,8 @@ def main():
     roofline = {"kernel": kname, "bound": "hbm",
                 "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "peak_source": f"{peak_kind} hbm_gbs",
-                "traffic": load_traffic(a.workload, T) if last_alg == g.ALG_SKL and team > 0 else None,
+                "traffic": (load_traffic(a.workload, T) if last_alg == g.ALG_SKL and team > 0 and not drive_override
+                            else None),  # (the committed captures are of the workloads' own drive)
                 "state_on_chip": resident,
                 "algorithmic_bytes_per_launch": (deliv_bytes + upd_bytes) / n_launch,
                 "launch_ms": kern_ms / n_launch,
