@@ -388,6 +388,8 @@ __device__ __forceinline__ int tagged_id(const unsigned long long *p, unsigned t
 // ---------------------------------------------------------------------------------------
 // One team member's share of one network for the steps of this launch.
 // ---------------------------------------------------------------------------------------
+constexpr int kUpd = 4;  // neurons a thread updates per round of the team kernel's update
+
 template <int NT, bool kPair>
 __device__ void team_run(const TeamItem &it, int rank, unsigned char *s_raw, TeamShared &sh,
                          unsigned long long limit_ns, int stall) {
@@ -436,7 +438,6 @@ __device__ void team_run(const TeamItem &it, int rank, unsigned char *s_raw, Tea
   float2 *vu = L.vu_sm ? s_vu : v.vu + lo;
   const float4 *abcd = L.abcd_sm ? s_abcd : v.abcd + lo;
   const float *rp = L.abcd_sm ? nullptr : (v.rpar ? v.rpar + lo : nullptr);  // a,b,c,d recomputed from r
-  auto param = [&](int i) -> float4 { return rp ? izh_abcd(rp[i], lo + i < v.nexc) : abcd[i]; };
 
   for (int i = threadIdx.x; i < cnt; i += NT) {
     const long long q = __ldcg(v.acc + lo + i);
@@ -467,36 +468,36 @@ __device__ void team_run(const TeamItem &it, int rank, unsigned char *s_raw, Tea
       v.base[lt] = base;
       if (v.stamps) v.stamps[2 * lt] = globaltimer();
     }
-    // ---- update of the owned neurons, two per thread per round with the loads first
-    for (int i0 = threadIdx.x; i0 < cnt; i0 += 2 * NT) {
-      const int i1 = i0 + NT;
-      const bool h1 = i1 < cnt;
-      const int j1 = h1 ? i1 : i0;
-      const int64_t n0 = lo + i0, n1 = lo + j1;
-      float2 s0 = vu[i0], s1 = vu[j1];
-      const float4 p0 = param(i0), p1 = param(j1);
-      const long long a0 = (long long)s_a[i0] * 65536 + s_b[i0];
-      const long long a1 = h1 ? (long long)s_a[i1] * 65536 + s_b[i1] : 0;
-      s_a[i0] = 0;
-      s_b[i0] = 0;
-      if (h1) {
-        s_a[i1] = 0;
-        s_b[i1] = 0;
+    // ---- update of the owned neurons, four per thread per round: the state loads of all
+    // four first (a slice whose state lives in global memory takes one memory round trip
+    // per round), then each neuron in turn
+    const bool use_z = L.prez && lt > 0;
+    for (int i0 = threadIdx.x; i0 < cnt; i0 += kUpd * NT) {
+      float2 sv[kUpd];
+      float rr[kUpd];
+#pragma unroll
+      for (int u = 0; u < kUpd; ++u) {
+        const int i = i0 + u * NT, j = i < cnt ? i : i0;
+        sv[u] = vu[j];
+        rr[u] = rp ? rp[j] : 0.0f;
       }
-      const bool use_z = L.prez && lt > 0;
-      const float z0 = use_z ? s_z[i0] : normal(v.seed, (uint64_t)n0, (uint64_t)t_abs);
-      const float z1 = use_z ? (h1 ? s_z[i1] : 0.0f) : normal(v.seed, (uint64_t)n1, (uint64_t)t_abs);
-      float I0, I1;
-      const bool k0 = izh_step(s0.x, s0.y, I0, p0, n0 < v.nexc ? v.ge : v.gi, z0, a0);
-      const bool k1 = izh_step(s1.x, s1.y, I1, p1, n1 < v.nexc ? v.ge : v.gi, z1, a1) && h1;
-      vu[i0] = s0;
-      if (h1) vu[i1] = s1;
-      if (last) {
-        v.ilast[n0] = I0;
-        if (h1) v.ilast[n1] = I1;
+#pragma unroll
+      for (int u = 0; u < kUpd; ++u) {
+        const int i = i0 + u * NT;
+        if (i < cnt) {
+          const int64_t nn = lo + i;
+          const float4 p = rp ? izh_abcd(rr[u], nn < v.nexc) : abcd[i];
+          const long long a = (long long)s_a[i] * 65536 + s_b[i];
+          s_a[i] = 0;
+          s_b[i] = 0;
+          const float z = use_z ? s_z[i] : normal(v.seed, (uint64_t)nn, (uint64_t)t_abs);
+          float I;
+          const bool k = izh_step(sv[u].x, sv[u].y, I, p, nn < v.nexc ? v.ge : v.gi, z, a);
+          vu[i] = sv[u];
+          if (last) v.ilast[nn] = I;
+          if (k) s_own[atomicAdd(&sh.nown[par], 1)] = (int)nn;
+        }
       }
-      if (k0) s_own[atomicAdd(&sh.nown[par], 1)] = (int)n0;
-      if (k1) s_own[atomicAdd(&sh.nown[par], 1)] = (int)n1;
     }
     __syncthreads();
     const int nown = sh.nown[par];
