@@ -71,3 +71,17 @@ def test_reference_arm_prints_from_rank_zero_only():
     assert line["impl"] == "reference" and line["n_gpus"] == 2 and line["value"] > 0
     assert line["cpu_baseline"]["kind"] == "port" and line["e2e"]["h2d_bytes_per_step"] == 0
     assert res[1].stdout.strip() == ""
+
+
+def test_reference_arm_at_another_drive():
+    """`--drive` replaces the workload's drive scale: the line's config says so, and the quiet
+    regime (0.5) fires far less than the balanced one on the same network."""
+    rates = {}
+    for drive in ("0.5", "1.0"):
+        r = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--workload", "n2500", "--drive", drive,
+                            "--steps", "1", "--warmup", "3"], cwd=ROOT, capture_output=True, text=True, timeout=240)
+        assert r.returncode == 0, r.stderr
+        line = json.loads([l for l in r.stdout.splitlines() if l.strip()][-1])
+        assert line["config"]["drive_scale"] == float(drive)
+        rates[drive] = line["value"]
+    assert rates["0.5"] < 0.1 * rates["1.0"]
