@@ -1,21 +1,23 @@
 // g4s_noalloc.cu — g4s_run_noalloc: the SKL team kernel on caller-owned device arrays,
 // without any allocation.
 //
-// Some callers cannot call cudaMalloc while they step a network: code running inside a
-// stream capture of someone else's CUDA graph (allocation calls are not capturable),
-// real-time loops that must not pay the device-wide synchronisation an allocation may
-// imply, and hosts whose device memory is owned by a capped pool that this library cannot
-// draw from.  For them this entry point uses only memory it already has: the caller
-// passes the network's arrays and the output buffers, and the kernel's scratch (the
-// team's per-step spike records and overflow ids, the per-row segment table of a
-// multi-CTA team, the error word and the work-queue words) lives in one file-scope
-// __device__ array of fixed size, which every GPU that loads the library holds until
-// the process exits.
+// Some callers cannot call cudaMalloc while they step a network: real-time loops that
+// must not pay the device-wide synchronisation an allocation or a free may imply, and
+// hosts whose device memory is owned by a capped pool that this library cannot draw
+// from.  For them this entry point uses only memory it already has: the caller passes the
+// network's arrays and the output buffers, and the kernel's scratch (the team's per-step
+// spike records and overflow ids, the per-row segment table of a multi-CTA team, the error
+// word and the work-queue words) lives in one file-scope __device__ array of fixed size,
+// which every GPU that loads the library holds until the process exits.  The call copies
+// nothing from host memory: the launch descriptor reaches the device as a kernel argument.
 //
 // Limits: at most kNoAllocMaxNeurons neurons and kNoAllocMaxTeam CTAs, and at most 16384
 // neurons per CTA (the shared-memory slice of the team kernel).  Every call shares the
 // scratch array and leaves its contents behind; calls that overlap on the GPU (on
 // different streams, or without ordering between them) race on it and must not be made.
+// A multi-CTA call rebuilds the per-row segment table from the caller's tables (a binary
+// search of every row per team boundary, reading about team x log2(stride) targets a row),
+// since it cannot know whether they changed since the last call.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -47,6 +49,23 @@ constexpr size_t kScratchBytes = kOffSeg + (size_t)kNoAllocMaxNeurons * (kNoAllo
 static_assert(sizeof(GridSync) <= kOffRec - kOffSync, "error word");
 static_assert(sizeof(int2) * kNoAllocMaxTeam <= kOffItem - kOffSlots, "slots");
 static_assert(sizeof(TeamItem) <= kOffList - kOffItem, "item");
+static_assert(kNoAllocMaxTeam <= 32, "one setup thread per slot");
+// about 6.5 MB: the documented size of the array in gpu4snn.h
+static_assert(kScratchBytes > 6400000 && kScratchBytes < 6600000, "scratch size as documented");
+
+// Writes the work-queue words, the team's slots and the launch descriptor into the
+// scratch array.  The descriptor arrives by value as a kernel argument, so the call stages
+// nothing through host memory.
+__global__ void k_noalloc_setup(TeamItem item, int *ctl, int2 *slots, TeamItem *dst) {
+  const int r = threadIdx.x;
+  if (r < item.team) slots[r] = make_int2(0, r);
+  if (r == 0) {
+    ctl[0] = item.team;  // slots in the queue
+    ctl[1] = 0;          // queue head
+    ctl[2] = 0;          // status word
+    *dst = item;
+  }
+}
 
 }  // namespace
 
@@ -146,18 +165,15 @@ extern "C" int g4s_run_noalloc(const g4s_dev_net *d, int64_t t_abs0, int32_t ste
   h.team = team;
   h.rc = (int)rc;
   h.sync = sync;
-  int2 hs[kNoAllocMaxTeam];
-  for (int r = 0; r < team; ++r) hs[r] = make_int2(0, r);
-  const int hc[2] = {team, 0};
-
   // Everything that must start at zero: error word, spike records and overflow ids (their
-  // tags restart with every call), queue head, step counts.
+  // tags restart with every call), step counts; then the queue words and the descriptor.
   cudaError_t e = cudaMemsetAsync(scr, 0, kOffSlots, s);
   if (e == cudaSuccess && team > 1) e = cudaMemsetAsync(list, 0, (size_t)d->n * 4 * sizeof(unsigned long long), s);
   if (e == cudaSuccess) e = cudaMemsetAsync(d_counts, 0, (size_t)steps * sizeof(int32_t), s);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(ctl, hc, sizeof hc, cudaMemcpyHostToDevice, s);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(slots, hs, sizeof(int2) * team, cudaMemcpyHostToDevice, s);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(item, &h, sizeof h, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) {
+    k_noalloc_setup<<<1, 32, 0, s>>>(h, ctl, slots, item);
+    e = cudaGetLastError();
+  }
   if (e == cudaSuccess && team > 1) e = launch_segoff(v, team, rc, seg, s);
   if (e == cudaSuccess)
     e = launch_team(item, slots, ctl, ctl + 1, team, team_smem(rc, team), 2000000000ull, 0, s, false);

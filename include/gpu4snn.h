@@ -268,19 +268,20 @@ typedef struct g4s_dev_net {
 
 /* The SKL team kernel on caller-owned device arrays, allocating nothing.  No counterpart
  * in the reference.  For callers that cannot allocate device memory while they step a
- * network: code inside a stream capture of another library's CUDA graph, real-time loops
- * that cannot take an allocation's device-wide synchronisation, hosts whose device memory
- * is a capped pool this library cannot draw from.  Advances `steps` steps from absolute
+ * network: real-time loops that cannot take the device-wide synchronisation an allocation
+ * or a free may imply, and hosts whose device memory is a capped pool this library cannot
+ * draw from.  Nothing is copied from host memory either.  Advances `steps` steps from absolute
  * step t_abs0 with a team of `team` CTAs (1..8); outputs, all device memory of the caller:
  * d_counts int32[steps] spikes per step, d_base int64[steps] raster offset of each step,
  * d_raster int32[raster_cap] spike ids (ids that do not fit are not recorded), d_status
  * (may be NULL) 0 or a device error code; `last` = 1 records i_last at the last step.
  * Stream-ordered on `stream` (NULL: the default stream).  The kernel's scratch is one
- * fixed __device__ array of about 3.4 MB (held by every GPU that loads the library): at
+ * fixed __device__ array of about 6.5 MB (held by every GPU that loads the library): at
  * most 131072 neurons and 16384 neurons per CTA; larger requests are rejected with
- * G4S_ERR_INVALID.  The first call on a device looks the array's address up, so make it
- * before any stream capture.  All calls share the array: calls that overlap on the GPU
- * race and must not be made. */
+ * G4S_ERR_INVALID.  The first call on a device looks the array's address up (once per
+ * device, with that device current) and sets the team kernel's shared-memory ceiling.  A
+ * multi-CTA call rebuilds the per-row segment table of its tables every time.  All calls
+ * share the array: calls that overlap on the GPU race and must not be made. */
 int g4s_run_noalloc(const g4s_dev_net *net, int64_t t_abs0, int32_t steps, int32_t team, int32_t last,
                     int32_t *d_counts, int64_t *d_base, int32_t *d_raster, int64_t raster_cap, int32_t *d_status,
                     void *stream);

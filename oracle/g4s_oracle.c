@@ -298,7 +298,8 @@ struct g4o_sim {
   float *v, *u, *ilast;
   int64_t *acc;
   /* FP64 state */
-  double *v64, *u64, *acc64;
+  double *v64, *u64;
+  __int128 *acc64; /* FP64 mode: exact Q64.64 sums of the weights */
   float *a, *b, *c, *dd;
   int32_t *nospks, *last;
   int64_t *nisi, *sisi, *sisi2;
@@ -331,7 +332,7 @@ g4o_sim *g4o_sim_create(const g4o_desc *d, const int32_t *idx, const float *w, i
   s->acc = xcalloc(n, 8);
   s->v64 = xcalloc(n, 8);
   s->u64 = xcalloc(n, 8);
-  s->acc64 = xcalloc(n, 8);
+  s->acc64 = xcalloc(n, sizeof(__int128));
   s->a = xcalloc(n, 4);
   s->b = xcalloc(n, 4);
   s->c = xcalloc(n, 4);
@@ -431,12 +432,19 @@ static inline int update32(g4o_sim *s, int64_t i, int32_t t) {
   return spk;
 }
 
+/* FP64 currents: each weight as an exact Q64.64 integer (every float weight of magnitude
+ * >= 2^-41 is exact; smaller ones round to nearest even), summed without rounding, and
+ * converted to double once, correctly rounded, when the neuron consumes them.  The sum
+ * therefore does not depend on the order of the additions. */
+static inline __int128 wq64(float w) { return (__int128)rint(ldexp((double)w, 64)); }
+static inline double q64_to_double(__int128 q) { return (double)q * 0x1p-64; }
+
 /* The same step in double with the same random draws. */
 static inline int update64(g4o_sim *s, int64_t i, int32_t t) {
   float z = g4o_normal(s->d.seed, (uint64_t)i, (uint64_t)t);
   double g = i < s->nexc ? (double)s->ge : (double)s->gi;
-  double I = g * (double)z + s->acc64[i];
-  s->acc64[i] = 0.0;
+  double I = g * (double)z + q64_to_double(s->acc64[i]);
+  s->acc64[i] = 0;
   double v = s->v64[i], u = s->u64[i];
   v += 0.5 * (0.04 * v * v + 5.0 * v + 140.0 - u + I);
   v += 0.5 * (0.04 * v * v + 5.0 * v + 140.0 - u + I);
@@ -477,7 +485,7 @@ int g4o_sim_run(g4o_sim *s, int32_t steps, int32_t threads) {
     s->ccap = cap;
   }
   int nth = threads < 1 ? 1 : threads;
-  if (s->mode == G4O_FP64) nth = 1; /* keep the double sums in one fixed order */
+  if (s->mode == G4O_FP64) nth = 1; /* the FP64 mode runs on one thread */
   for (int32_t st = 0; st < steps; ++st) {
     const int32_t t = (int32_t)s->t;
     int64_t k = 0;
@@ -545,7 +553,7 @@ int g4o_sim_run(g4o_sim *s, int32_t steps, int32_t threads) {
         const float *rw = s->w + row * stride;
         if (s->mode == G4O_FP64) {
           for (int64_t j = 0; j < stride; ++j)
-            if (ri[j] >= 0) s->acc64[ri[j]] += (double)rw[j];
+            if (ri[j] >= 0) s->acc64[ri[j]] += wq64(rw[j]);
         } else {
           for (int64_t j = 0; j < stride; ++j)
             if (ri[j] >= 0) s->acc[ri[j]] += g4o_wfix(rw[j]);

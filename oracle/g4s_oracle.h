@@ -19,8 +19,11 @@
  * Two arithmetic modes:
  *   G4O_FP32  — the FP32 mirror: every float operation in the same order and rounding
  *               as the CUDA kernels; rasters, states and currents are bit-exact.
- *   G4O_FP64  — the same random draws promoted to double, dynamics and currents in
- *               double; used to bound the FP32 error of the membrane potential.
+ *   G4O_FP64  — the same random draws promoted to double, dynamics in double; the
+ *               synaptic currents are exact Q64.64 sums of the weights, converted to
+ *               double (correctly rounded) when consumed, so they do not depend on the
+ *               order of the additions; used to bound the FP32 error of the membrane
+ *               potential, and the CPU twin of the library's on-device FP64 check.
  *
  * Pinning: Philox4x64-10 against numpy.random.Philox; the reference-compatible table
  * generator (glibc rand) against tables dumped by the reference's own host code.

@@ -34,8 +34,9 @@ class Desc(C.Structure):
 
 
 def build(force: bool = False) -> str:
-    """Compile the oracle with make (gcc, -ffp-contract=off)."""
-    if force or not os.path.exists(LIB_PATH):
+    """Compile the oracle and the reference-kernel harness with make (gcc, -ffp-contract=off)."""
+    harness = os.path.join(HERE, "_build", "g4s_refgpu")
+    if force or not os.path.exists(LIB_PATH) or not os.path.exists(harness):
         subprocess.run(["make", "-s", "-C", HERE], check=True)
     return LIB_PATH
 

@@ -1,12 +1,15 @@
 """g4s_run_noalloc, the allocation-free entry point, against g4s_net_run.
 
 The entry point exists for callers that cannot allocate device memory while they step a
-network (inside another library's stream capture, in real-time loops, under a capped
-memory pool): it runs the SKL team kernel on device arrays the caller owns and keeps its
-own scratch in a fixed device array.  Here the caller's arrays are torch tensors built
-from a handle's initial state and sorted tables; two calls in a row must give exactly the
-rasters, states and pending currents of two g4s_net_run calls on an identical handle.
-This file is collected last so that a failure here cannot hide the other tests.
+network (real-time loops that cannot take an allocation's device-wide synchronisation,
+hosts whose device memory is a capped pool): it runs the SKL team kernel on device arrays
+the caller owns and keeps its own scratch in a fixed device array.  Here the caller's
+arrays are torch tensors built from a handle's initial state and sorted tables; two calls
+in a row must give exactly the rasters, states and pending currents of two g4s_net_run
+calls on an identical handle.  The cases cover one CTA, a two-CTA team, and a team of 8
+at the 131072-neuron limit driven hard enough that a step's spikes overflow the rank's
+shared-memory window (the tagged dense-list path, whose words the second call must find
+cleared).  This file is collected last so that a failure here cannot hide the other tests.
 """
 import ctypes as C
 
@@ -33,13 +36,14 @@ def _raster(counts, base, raster, t0):
     return np.concatenate(t), np.concatenate(ids)
 
 
-@pytest.mark.parametrize("n,nsyn,team", [(20000, 300, 2), (6000, 1000, 1)])
-def test_noalloc_matches_net_run(g4s, n, nsyn, team):
+@pytest.mark.parametrize("n,nsyn,team,drive", [(20000, 300, 2, 1.0), (6000, 1000, 1, 1.0), (131072, 100, 8, 2.0)])
+def test_noalloc_matches_net_run(g4s, n, nsyn, team, drive):
     torch = pytest.importorskip("torch")
     from gpu4snn_gb300 import _lib
     L = _lib.load()
     seed, steps, dev = 41, 60, "cuda:0"
-    with g4s.Network(n, nsyn, seed=seed) as ref, g4s.Network(n, nsyn, seed=seed) as src:
+    with g4s.Network(n, nsyn, seed=seed, drive_scale=drive) as ref, \
+            g4s.Network(n, nsyn, seed=seed, drive_scale=drive) as src:
         st = src.state()
         idx, w = src.tables()
         vu = torch.tensor(np.stack([st["v"], st["u"]], 1), device=dev)
@@ -54,7 +58,8 @@ def test_noalloc_matches_net_run(g4s, n, nsyn, team):
         base = torch.zeros(steps, dtype=torch.int64, device=dev)
         raster = torch.zeros(n * steps, dtype=torch.int32, device=dev)
         status = torch.ones(1, dtype=torch.int32, device=dev)
-        d = DevNet(n=n, nexc=n * 800 // 1000, nsyn=nsyn, stride=idx.shape[1], seed=seed, ge=5.0, gi=2.0,
+        d = DevNet(n=n, nexc=n * 800 // 1000, nsyn=nsyn, stride=idx.shape[1], seed=seed,
+                   ge=float(np.float32(5.0) * np.float32(drive)), gi=float(np.float32(2.0) * np.float32(drive)),
                    vu=vu.data_ptr(), abcd=abcd.data_ptr(), acc=acc.data_ptr(), i_last=ilast.data_ptr(),
                    spike_stat=sstat.data_ptr(), idx=tidx.data_ptr(), w=tw.data_ptr())
         torch.cuda.synchronize()
@@ -67,6 +72,10 @@ def test_noalloc_matches_net_run(g4s, n, nsyn, team):
             ref.run(steps, g4s.ALG_SKL)
             rt, rid = ref.raster()
             sel = rt >= call * steps
+            if team == 8:
+                # the case exists for the dense-list path: a step with more spikes than the
+                # rank's shared-memory window (1728 ids at 16384 neurons per CTA)
+                assert np.bincount(rt[sel] - call * steps).max() > 1728
             t, ids = _raster(counts.cpu().numpy(), base.cpu().numpy(), raster.cpu().numpy(), call * steps)
             assert np.array_equal(t, rt[sel]) and np.array_equal(ids, rid[sel])
         s = ref.state()
