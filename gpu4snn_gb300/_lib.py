@@ -121,6 +121,7 @@ SIGNATURES = [
     ("g4s_run_protocol", C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_uint64,
                                    C.c_int32, C.c_char_p]),
     ("g4s_conn_glibc", C.c_int, [C.c_uint32, C.c_int32, C.c_int32, C.c_int32, _P, _P]),
+    ("g4s_net_fp64_check", C.c_int, [_P, C.c_int32, _P, _P, _P, C.POINTER(C.c_int32), _P, _P]),
     ("g4s_run_noalloc", C.c_int, [_P, C.c_int64, C.c_int32, C.c_int32, C.c_int32, _P, _P, _P, C.c_int64, _P, _P]),
     ("g4s_server_start", C.c_int, [C.c_int64, C.c_int32, C.POINTER(_P)]),
     ("g4s_server_submit", C.c_int, [_P, C.POINTER(Request), C.POINTER(C.c_int64)]),

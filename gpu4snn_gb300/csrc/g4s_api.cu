@@ -499,6 +499,10 @@ double net_recent_step_ms(const g4s_net *n, int64_t k) {
   return used ? sum / (double)used : 0.0;
 }
 
+const NetView &net_view(const g4s_net *n) { return n->v; }
+cudaStream_t net_stream(const g4s_net *n) { return n->stream; }
+int64_t net_steps_done(const g4s_net *n) { return n->t_abs; }
+
 }  // namespace g4s
 
 // ---------------------------------------------------------------------------------------

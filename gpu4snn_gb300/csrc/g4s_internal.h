@@ -170,6 +170,12 @@ cudaError_t team_smem_ceiling();  // the part of team_max_blocks that launch_tea
 // shared memory of one rank of a team of `team` CTAs with `rc` neurons each (0: does not fit)
 size_t team_smem(int64_t rc, int team);
 
+// A handle's arrays, stream and absolute step, for the library's other translation units
+// (the on-device FP64 check, g4s_fp64check.cu).
+const NetView &net_view(const g4s_net *n);
+cudaStream_t net_stream(const g4s_net *n);
+int64_t net_steps_done(const g4s_net *n);
+
 // Binary files (g4s_formats.cu): the raster, streamed by a writer thread, and the tables.
 struct RasterFile;
 int raster_open(const char *path, int64_t n, int64_t t0, RasterFile **out);

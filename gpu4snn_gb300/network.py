@@ -173,6 +173,18 @@ class Network:
         check(load().g4s_net_stats(self._h, C.byref(r), C.byref(cv), C.byref(tot)))
         return Stats(r.value, cv.value, tot.value)
 
+    def fp64_check(self, steps: int) -> dict:
+        """On-device FP64 check (g4s_net_fp64_check): from step 0, `steps` steps of this
+        network in lockstep with an FP64 twin on the GPU.  Returns per-step max, p99 and
+        median |v32 - v64| (mV), the first step whose spike sets differ (-1: none) and the
+        twin's final v, u."""
+        mx, p99, p50 = (np.zeros(steps) for _ in range(3))
+        v64, u64 = np.empty(self.n), np.empty(self.n)
+        first = C.c_int32()
+        check(load().g4s_net_fp64_check(self._h, steps, ptr(mx), ptr(p99), ptr(p50), C.byref(first), ptr(v64),
+                                        ptr(u64)))
+        return {"max": mx, "p99": p99, "median": p50, "first_divergent": first.value, "v64": v64, "u64": u64}
+
     def write_results(self, directory: str, elapsed_ms: float, elapsed_with_data_ms: float):
         check(load().g4s_net_write_results(self._h, directory.encode(), None, elapsed_ms, elapsed_with_data_ms))
 

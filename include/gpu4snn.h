@@ -115,6 +115,17 @@ int g4s_net_currents(g4s_net *net, int64_t *acc);
 int g4s_net_tables(g4s_net *net, int64_t row0, int64_t nrows, int32_t *idx, float *w);
 /* FP64 statistics: mean rate (Hz, 1 ms steps) and mean per-neuron ISI CV. */
 int g4s_net_stats(g4s_net *net, double *rate_hz, double *isi_cv, int64_t *total_spikes);
+/* On-device FP64 check of the network's FP32 trajectory (no counterpart in the reference,
+ * whose update, gpu4snn.cu:376-405, runs in FP32 only): from step 0 (after create or
+ * reset; G4S_ERR_STATE otherwise) runs `steps` steps of the network (SKL scheme) in
+ * lockstep with an FP64 twin on the GPU: the same random draws, v and u in double, the
+ * synaptic currents as exact Q64.64 sums (the CPU oracle's FP64 mode, bit for bit).  Per
+ * step t: dv_max[t], dv_p99[t], dv_median[t] = max, 99th and 50th nearest-rank percentile
+ * of |v32 - v64| (mV) over all neurons; *first_divergent = first step whose spike sets
+ * differ (-1: none); v64_out, u64_out [n] = the twin's final state.  Any output may be
+ * NULL.  The network advances by `steps` steps.  Allocates ~41 bytes per neuron. */
+int g4s_net_fp64_check(g4s_net *net, int32_t steps, double *dv_max, double *dv_p99, double *dv_median,
+                       int32_t *first_divergent, double *v64_out, double *u64_out);
 /* Grid-barrier time limit of the SKL kernel in ns (default 2 s); 0 makes every barrier
  * give up at once (used to test the timeout path). */
 int g4s_net_set_barrier_timeout(g4s_net *net, uint64_t ns);
