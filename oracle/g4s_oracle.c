@@ -203,50 +203,109 @@ static inline int64_t n_exc_of(const g4o_desc *d) { return (d->n * (int64_t)d->e
  * excitatory rows, (1000/nsyn)*(-1)*U for inhibitory ones, U = 24-bit uniform of word
  * j%4 of Philox(row, j/4) — the reference's law at gpu4snn.cu:887-898.
  * ------------------------------------------------------------------------------- */
+/* One row of the Philox law into ri/rw; `mark` (n words) remembers the rows that took each
+ * target, so it needs no clearing between rows. */
+static void conn_philox_row(const g4o_desc *d, int64_t row, int64_t nexc, int64_t *mark, int32_t *ri, float *rw) {
+  const int32_t nsyn = d->nsyn, stride = d->stride;
+  const float wscale = 1000.0f / (float)nsyn;
+  const float wexc = wscale * 0.5f, winh = wscale * -1.0f;
+  const uint64_t range = d->self_loops ? (uint64_t)d->n : (uint64_t)(d->n - 1);
+  int32_t acc = 0;
+  for (uint64_t b = 0; acc < nsyn; ++b) {
+    uint64_t blk[32][4];
+    for (int l = 0; l < 32; ++l) philox(d->seed, G4O_STREAM_CONN, (uint64_t)row, 32u * b + (uint64_t)l, 0, blk[l]);
+    for (int r = 0; r < 4 && acc < nsyn; ++r)
+      for (int l = 0; l < 32 && acc < nsyn; ++l) {
+        uint64_t hi, lo;
+        mulhilo64(blk[l][r], range, &hi, &lo);
+        int64_t t = (int64_t)hi;
+        if (!d->self_loops && t >= row) t += 1;
+        if (mark[t] != row) {
+          mark[t] = row;
+          ri[acc++] = (int32_t)t;
+        }
+      }
+  }
+  const float sc = row < nexc ? wexc : winh;
+  for (int32_t j = 0; j < nsyn; j += 4) {
+    uint64_t o[4];
+    philox(d->seed, G4O_STREAM_WEIGHT, (uint64_t)row, (uint64_t)(j >> 2), 0, o);
+    for (int q = 0; q < 4 && j + q < nsyn; ++q) rw[j + q] = sc * u24(o[q]);
+  }
+  for (int32_t j = nsyn; j < stride; ++j) {
+    ri[j] = -1;
+    rw[j] = 0.0f;
+  }
+}
+
 int g4o_conn_philox(const g4o_desc *d, int64_t row0, int64_t nrows, int32_t *idx, float *w) {
   const int64_t n = d->n;
   const int32_t nsyn = d->nsyn, stride = d->stride;
   if (n < 2 || nsyn < 0 || stride < nsyn || nsyn > (d->self_loops ? n : n - 1)) return -1;
   const int64_t nexc = n_exc_of(d);
-  const float wscale = 1000.0f / (float)nsyn;
-  const float wexc = wscale * 0.5f, winh = wscale * -1.0f;
-  int64_t *mark = (int64_t *)malloc((size_t)n * sizeof(int64_t));
-  if (!mark) return -1;
-  for (int64_t i = 0; i < n; ++i) mark[i] = -1;
-  const uint64_t range = d->self_loops ? (uint64_t)n : (uint64_t)(n - 1);
-  for (int64_t rr = 0; rr < nrows; ++rr) {
-    const int64_t row = row0 + rr;
-    int32_t *ri = idx + rr * (int64_t)stride;
-    float *rw = w + rr * (int64_t)stride;
-    int32_t acc = 0;
-    for (uint64_t b = 0; acc < nsyn; ++b) {
-      uint64_t blk[32][4];
-      for (int l = 0; l < 32; ++l) philox(d->seed, G4O_STREAM_CONN, (uint64_t)row, 32u * b + (uint64_t)l, 0, blk[l]);
-      for (int r = 0; r < 4 && acc < nsyn; ++r)
-        for (int l = 0; l < 32 && acc < nsyn; ++l) {
-          uint64_t hi, lo;
-          mulhilo64(blk[l][r], range, &hi, &lo);
-          int64_t t = (int64_t)hi;
-          if (!d->self_loops && t >= row) t += 1;
-          if (mark[t] != row) {
-            mark[t] = row;
-            ri[acc++] = (int32_t)t;
-          }
-        }
-    }
-    const float sc = row < nexc ? wexc : winh;
-    for (int32_t j = 0; j < nsyn; j += 4) {
-      uint64_t o[4];
-      philox(d->seed, G4O_STREAM_WEIGHT, (uint64_t)row, (uint64_t)(j >> 2), 0, o);
-      for (int q = 0; q < 4 && j + q < nsyn; ++q) rw[j + q] = sc * u24(o[q]);
-    }
-    for (int32_t j = nsyn; j < stride; ++j) {
-      ri[j] = -1;
-      rw[j] = 0.0f;
+  int failed = 0;
+  /* rows are independent: blocks of rows on all threads, each with its own mark array */
+#pragma omp parallel if (nrows > 256)
+  {
+    int64_t *mark = (int64_t *)malloc((size_t)n * sizeof(int64_t));
+    if (!mark) {
+#pragma omp atomic write
+      failed = 1;
+    } else {
+      for (int64_t i = 0; i < n; ++i) mark[i] = -1;
+#pragma omp for schedule(dynamic, 64)
+      for (int64_t rr = 0; rr < nrows; ++rr)
+        conn_philox_row(d, row0 + rr, nexc, mark, idx + rr * (int64_t)stride, w + rr * (int64_t)stride);
+      free(mark);
     }
   }
-  free(mark);
-  return 0;
+  return failed ? -1 : 0;
+}
+
+/* Rows in the library's order: by target as unsigned (so unused slots, -1, come last),
+ * equal targets by the weight's bits; a least-significant-digit radix sort of the 64-bit
+ * keys (target << 32 | weight bits), rows on all threads. */
+int g4o_sort_rows(int32_t *idx, float *w, int64_t nrows, int32_t stride) {
+  int failed = 0;
+#pragma omp parallel if (nrows > 64)
+  {
+    uint64_t *a = (uint64_t *)malloc((size_t)stride * 8), *b = (uint64_t *)malloc((size_t)stride * 8);
+    if (!a || !b) {
+#pragma omp atomic write
+      failed = 1;
+    } else {
+#pragma omp for schedule(dynamic, 64)
+      for (int64_t r = 0; r < nrows; ++r) {
+        int32_t *ri = idx + r * (int64_t)stride;
+        float *rw = w + r * (int64_t)stride;
+        for (int32_t j = 0; j < stride; ++j) {
+          uint32_t wb;
+          memcpy(&wb, rw + j, 4);
+          a[j] = ((uint64_t)(uint32_t)ri[j] << 32) | wb;
+        }
+        uint64_t *src = a, *dst = b;
+        for (int pass = 0; pass < 8; ++pass) {
+          const int sh = 8 * pass;
+          uint32_t cnt[257] = {0};
+          for (int32_t j = 0; j < stride; ++j) cnt[((src[j] >> sh) & 0xFF) + 1]++;
+          if (cnt[((src[0] >> sh) & 0xFF) + 1] == (uint32_t)stride) continue; /* one digit value: order kept */
+          for (int k = 0; k < 256; ++k) cnt[k + 1] += cnt[k];
+          for (int32_t j = 0; j < stride; ++j) dst[cnt[(src[j] >> sh) & 0xFF]++] = src[j];
+          uint64_t *t = src;
+          src = dst;
+          dst = t;
+        }
+        for (int32_t j = 0; j < stride; ++j) {
+          ri[j] = (int32_t)(uint32_t)(src[j] >> 32);
+          const uint32_t wb = (uint32_t)src[j];
+          memcpy(rw + j, &wb, 4);
+        }
+      }
+    }
+    free(a);
+    free(b);
+  }
+  return failed ? -1 : 0;
 }
 
 /* The reference's host generator (gpu4snn.cu:873-898): srand(seed); per row a fresh

@@ -69,6 +69,9 @@ int64_t g4o_conn_draw(uint64_t seed, int64_t n, int self_loops, int64_t row, int
 /* Philox law: rows [row0, row0+nrows), written at idx/w + (row-row0)*stride.
  * Slots nsyn..stride-1 are padding (idx -1, w 0). Returns 0 or -1. */
 int g4o_conn_philox(const g4o_desc *d, int64_t row0, int64_t nrows, int32_t *idx, float *w);
+/* Rows sorted in the library's order: by target as unsigned (padding -1 last), equal
+ * targets by weight bits.  Returns 0 or -1. */
+int g4o_sort_rows(int32_t *idx, float *w, int64_t nrows, int32_t stride);
 /* The reference's own law with glibc rand() after srand(seed) (gpu4snn.cu:873-898). */
 int g4o_conn_glibc(unsigned seed, int32_t n, int32_t nsyn, int32_t *idx, float *w);
 /* Q32.32 value of one weight */

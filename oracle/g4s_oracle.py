@@ -62,6 +62,7 @@ def lib():
         L.g4o_conn_draw.restype = C.c_int64
         L.g4o_conn_philox.argtypes = [C.POINTER(Desc), C.c_int64, C.c_int64, p, p]
         L.g4o_conn_glibc.argtypes = [C.c_uint, C.c_int32, C.c_int32, p, p]
+        L.g4o_sort_rows.argtypes = [p, p, C.c_int64, C.c_int32]
         L.g4o_wfix.argtypes = [C.c_float]
         L.g4o_wfix.restype = C.c_int64
         L.g4o_sim_create.argtypes = [C.POINTER(Desc), p, p, C.c_int]
@@ -133,6 +134,14 @@ def conn_philox(desc: Desc, row0: int = 0, nrows: int | None = None):
     if lib().g4o_conn_philox(C.byref(desc), row0, nrows, _ptr(idx), _ptr(w)) != 0:
         raise ValueError("invalid connectivity request")
     return idx, w
+
+
+def sort_rows(idx: np.ndarray, w: np.ndarray):
+    """Sort every row in place into the library's order (target as unsigned, then weight bits)."""
+    assert idx.flags.c_contiguous and w.flags.c_contiguous and idx.shape == w.shape
+    assert idx.dtype == np.int32 and w.dtype == np.float32
+    if lib().g4o_sort_rows(_ptr(idx), _ptr(w), idx.shape[0], idx.shape[1]) != 0:
+        raise MemoryError("row sort failed")
 
 
 def conn_glibc(seed: int, n: int, nsyn: int):
