@@ -14,10 +14,16 @@ persistent step kernel against the measured HBM copy bandwidth; `e2e` is the sam
 through the C ABI with host tables uploaded from pinned memory, a reset, the run and the
 raster read back, every step.  `cpu_baseline` is the oracle's OpenMP port on the host cores.
 
+`reference_gpu`: the reference's own CUDA kernels (gpu4snn.cu compiled unmodified for
+sm_103a into a cubin, driven by this project's harness oracle/refgpu/g4s_refgpu.c) on the
+same network's connectivity and drive mode, each of its five schemes timed with CUDA
+events, and the headline's speed-up over its best scheme.  `large`: the N=10^6 x 1000 and
+N=250,000 x 10,000 networks, each timed like the headline (its own roofline, clocks and
+DRAM traffic).  `e2e` runs as many steps as the timed leg.
+
 --impl reference times the reference's algorithm on the CPU (the oracle's OpenMP port of
-gpu4snn.cu's step, all host threads) on the same network; the reference itself has no CPU
-implementation of the step and its CUDA program cannot be built on the GPU host (its
-sources are not shipped there).
+gpu4snn.cu's step, all host threads) on the same network: the reference has no CPU
+implementation of the step (its kernels' GPU timings are the `reference_gpu` block).
 
 Multi-GPU: the path does not shard; `--gpus N` under torchrun runs N independent replicas
 (seed + rank), value = all ranks' events / the slowest rank's time ("scaling": "weak").
@@ -327,6 +333,113 @@ def load_traffic(name, steps_per_launch):
     return None
 
 
+def timed_leg(g, net, name, cfg, alg, a, pg, local, drive_override):
+    """W warm-up runs, then K timed runs of T steps (CUDA events on the library's stream,
+    clocks sampled meanwhile); returns the measured figures and the roofline of the step
+    kernel (algorithmic bytes per launch over the mean launch time)."""
+    n, nsyn, T, drive, seed = cfg
+    for _ in range(a.warmup):
+        net.run(T, alg)
+    runs = []
+    if pg:
+        pg.barrier()
+    with ClockSampler(local) as clk:
+        w0 = time.perf_counter()
+        for _ in range(a.steps):
+            net.run(T, alg)
+            inf = net.info()
+            u, s = net.step_times()
+            runs.append((inf.last_run_ms, inf.last_run_kernel_ms, inf.last_run_spikes, inf.last_run_launches,
+                         float(u[-T:].sum()), float(s[-T:].sum()), inf.last_algorithm))
+        wall = time.perf_counter() - w0
+    if pg:
+        pg.barrier()
+    dev_ms = sum(r[0] for r in runs)
+    kern_ms = sum(r[1] for r in runs)
+    spikes = sum(r[2] for r in runs)
+    launches = sum(r[3] for r in runs)
+    events = spikes * nsyn
+    peak, peak_kind = peaks()
+    team, slice_ = net.geometry()
+    last_alg = int(runs[-1][6])
+    resident = last_alg == g.ALG_SKL and team > 0 and slice_ <= RESIDENT_SLICE
+    deliv_bytes = events * 8
+    upd_bytes = spikes * STAT_BYTES_PER_SPIKE + (0 if resident else n * T * a.steps * UPDATE_BYTES_PER_NEURON)
+    n_launch = max(1, launches)
+    achieved = (deliv_bytes + upd_bytes) / n_launch / (kern_ms / n_launch * 1e-3) / 1e9
+    upd_ms = sum(r[4] for r in runs)
+    deliv_ms = max(1e-9, sum(r[5] for r in runs) - upd_ms)
+    if last_alg == g.ALG_SKL and team > 0:
+        kname = f"k_team (SKL team kernel: {team} CTAs x {net.block_threads()} threads, {slice_} neurons per CTA)"
+    elif last_alg == g.ALG_SKL:
+        kname = "k_persistent (SKL global-atomic kernel)"
+    else:
+        kname = f"k_update + k_deliver ({ALG_LABEL[last_alg]})"
+    roofline = {"kernel": kname, "bound": "hbm",
+                "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "peak_source": f"{peak_kind} hbm_gbs",
+                "traffic": (load_traffic(name, T) if last_alg == g.ALG_SKL and team > 0 and not drive_override
+                            else None),  # (the committed captures are of the workloads' own drive)
+                "state_on_chip": resident,
+                "algorithmic_bytes_per_launch": (deliv_bytes + upd_bytes) / n_launch,
+                "launch_ms": kern_ms / n_launch,
+                "delivery_phase": {"bytes": deliv_bytes, "ms": deliv_ms, "gbs": deliv_bytes / deliv_ms / 1e6,
+                                   "frac": deliv_bytes / deliv_ms / 1e6 / peak},
+                "update_phase": {"bytes": upd_bytes, "ms": upd_ms, "gbs": upd_bytes / max(upd_ms, 1e-9) / 1e6}}
+    return {"dev_ms": dev_ms, "spikes": spikes, "events": events, "launches": launches, "wall": wall,
+            "last_alg": last_alg, "roofline": roofline, "clocks": clk.summary()}
+
+
+def large_leg(g, a, local):
+    """The large single networks at their workloads' own drive, each on its own: N=10^6 x
+    1000 and N=250,000 x 10,000, SKL (the autotuner's pick for both), with the roofline of
+    that launch, its clocks and its DRAM traffic from the committed ncu summary."""
+    out = {}
+    for name in ("n1m", "n250k_s10k"):
+        cfg = WORKLOADS[name]
+        n, nsyn, T, drive, seed = cfg
+        t0 = time.perf_counter()
+        net = g.Network(n, nsyn, seed=seed, drive_scale=drive, record_raster=False)
+        create_s = time.perf_counter() - t0
+        r = timed_leg(g, net, name, cfg, g.ALG_SKL, a, None, local, False)
+        net.close()
+        out[name] = {"metric": "synaptic events/s", "value": r["events"] / (r["dev_ms"] * 1e-3), "unit": "events/s",
+                     "ms_per_step": r["dev_ms"] / a.steps, "us_per_sim_step": r["dev_ms"] * 1e3 / (a.steps * T),
+                     "steps": a.steps, "warmup": a.warmup, "firing_rate_hz": r["spikes"] / (n * T * a.steps) * 1e3,
+                     "config": workload_config(name, cfg), "create_s": create_s, "roofline": r["roofline"],
+                     "clocks": r["clocks"], "gpu_launches": int(r["launches"])}
+    return out
+
+
+def reference_gpu_leg(cfg, steps=1000):
+    """The reference's own CUDA kernels (gpu4snn.cu compiled unmodified for sm_103a) on this
+    GPU, on the same network's connectivity (the oracle's Philox rows, in draw order, as the
+    reference keeps its rows), its drive mode matching the workload's gains, one run of
+    `steps` steps per scheme after a warm-up run; "unavailable" when the cubin is absent."""
+    n, nsyn, T, drive, seed = cfg
+    modes = {0.5: 0, 1.0: 1, 1.5: 2}
+    from oracle import g4s_oracle as O
+    from oracle import refgpu as R
+    why = R.unavailable()
+    if why or drive not in modes:
+        return {"unavailable": why or f"drive scale {drive} is none of the reference's modes"}
+    if n * nsyn >= 2 ** 31:
+        return {"unavailable": "N x Nsyn >= 2^31 overflows the reference's int synapse indices"}
+    O.build()
+    idx, w = O.conn_philox(O.make_desc(n, nsyn, seed))
+    res = R.run(idx, w, steps=steps, schemes=(0, 1, 2, 3, 4), modes=(modes[drive],), seeds=(seed,), reps=2)
+    out = {"kind": "reference CUDA kernels, gpu4snn.cu unmodified, -O3 for sm_103a (cubin), "
+                   "driven by oracle/refgpu/g4s_refgpu.c", "mode": modes[drive], "steps": steps, "schemes": {}}
+    for r in res:
+        if r.get("rep") == 1:
+            out["schemes"][R.SCHEMES[r["scheme"]]] = {
+                "events_per_s": r["spikes"] * nsyn / (r["ms"] * 1e-3), "us_per_step": r["ms"] * 1e3 / steps,
+                "grid": r["grid"], "block": r["block"]}
+    best = max(out["schemes"].items(), key=lambda kv: kv[1]["events_per_s"])
+    out["best"] = {"scheme": best[0], **best[1]}
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -348,6 +461,8 @@ def main():
     ap.add_argument("--served", default="50,200,1000",
                     help="comma-separated Poisson arrival rates (req/s) for the served leg ('' skips it)")
     ap.add_argument("--served-requests", type=int, default=200, help="requests per arrival rate")
+    ap.add_argument("--no-large", action="store_true", help="skip the N=10^6 and 250k x 10k block")
+    ap.add_argument("--no-reference-gpu", action="store_true", help="skip the reference-kernel block")
     a = ap.parse_args()
     if a.warmup < 3:
         a.warmup = 3
@@ -378,58 +493,12 @@ def main():
         tuned = {"algorithm": talg, "name": ALG_LABEL[talg], "team": tteam, "us_per_step": tus}
         net.run(8, alg)  # (applies the choice, so that its CTA size can be read back)
         tuned["block_threads"] = net.block_threads()
-    for _ in range(a.warmup):
-        net.run(T, alg)
-    runs = []
-    if pg:
-        pg.barrier()
-    with ClockSampler(local) as clk:
-        w0 = time.perf_counter()
-        for _ in range(a.steps):
-            net.run(T, alg)
-            inf = net.info()
-            u, s = net.step_times()
-            runs.append((inf.last_run_ms, inf.last_run_kernel_ms, inf.last_run_spikes, inf.last_run_launches,
-                         float(u[-T:].sum()), float(s[-T:].sum()), inf.last_algorithm))
-        wall = time.perf_counter() - w0
-    if pg:
-        pg.barrier()
-    clocks = clk.summary()
-    dev_ms = sum(r[0] for r in runs)
-    kern_ms = sum(r[1] for r in runs)
-    spikes = sum(r[2] for r in runs)
-    launches = sum(r[3] for r in runs)
-    events = spikes * nsyn
-    t_max = reduce_max(pg, dev_ms)
-    ev_all = reduce_sum(pg, float(events))
+    r = timed_leg(g, net, a.workload, cfg, alg, a, pg, local, drive_override)
+    t_max = reduce_max(pg, r["dev_ms"])
+    ev_all = reduce_sum(pg, float(r["events"]))
     value = ev_all / (t_max * 1e-3)
-    peak, peak_kind = peaks()
-    team, slice_ = net.geometry()
-    last_alg = int(runs[-1][6])
-    resident = last_alg == g.ALG_SKL and team > 0 and slice_ <= RESIDENT_SLICE
-    deliv_bytes = events * 8
-    upd_bytes = spikes * STAT_BYTES_PER_SPIKE + (0 if resident else n * T * a.steps * UPDATE_BYTES_PER_NEURON)
-    n_launch = max(1, launches)
-    achieved = (deliv_bytes + upd_bytes) / n_launch / (kern_ms / n_launch * 1e-3) / 1e9
-    upd_ms = sum(r[4] for r in runs)
-    deliv_ms = max(1e-9, sum(r[5] for r in runs) - upd_ms)
-    if last_alg == g.ALG_SKL and team > 0:
-        kname = f"k_team (SKL team kernel: {team} CTAs x {net.block_threads()} threads, {slice_} neurons per CTA)"
-    elif last_alg == g.ALG_SKL:
-        kname = "k_persistent (SKL global-atomic kernel)"
-    else:
-        kname = f"k_update + k_deliver ({ALG_LABEL[last_alg]})"
-    roofline = {"kernel": kname, "bound": "hbm",
-                "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "peak_source": f"{peak_kind} hbm_gbs",
-                "traffic": (load_traffic(a.workload, T) if last_alg == g.ALG_SKL and team > 0 and not drive_override
-                            else None),  # (the committed captures are of the workloads' own drive)
-                "state_on_chip": resident,
-                "algorithmic_bytes_per_launch": (deliv_bytes + upd_bytes) / n_launch,
-                "launch_ms": kern_ms / n_launch,
-                "delivery_phase": {"bytes": deliv_bytes, "ms": deliv_ms, "gbs": deliv_bytes / deliv_ms / 1e6,
-                                   "frac": deliv_bytes / deliv_ms / 1e6 / peak},
-                "update_phase": {"bytes": upd_bytes, "ms": upd_ms, "gbs": upd_bytes / max(upd_ms, 1e-9) / 1e6}}
+    spikes, launches, wall, last_alg, roofline, clocks = (r["spikes"], r["launches"], r["wall"], r["last_alg"],
+                                                          r["roofline"], r["clocks"])
     line = {"metric": "synaptic events/s", "value": value, "unit": "events/s", "n_gpus": ws, "steps": a.steps,
             "warmup": a.warmup, "ms_per_step": t_max / a.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32+i64", "data": "synthetic (seeded Philox network)",
@@ -448,7 +517,7 @@ def main():
         e2e_net.reset()
         e2e_net.run(T, alg)
         e_ev, e_wall, d2h = 0, 0.0, 0
-        for _ in range(max(1, min(a.steps, 3))):
+        for _ in range(a.steps):
             t0 = time.perf_counter()
             e2e_net.load_tables(idx_h, w_h)
             e2e_net.reset()
@@ -458,7 +527,7 @@ def main():
             e_wall += time.perf_counter() - t0
             e_ev += len(rt) * nsyn
             d2h = len(rt) * 4 + T * (4 + 8 + 16)
-        k = max(1, min(a.steps, 3))
+        k = a.steps
         e_wall = reduce_max(pg, e_wall)
         line["e2e"] = {"value": reduce_sum(pg, float(e_ev)) / e_wall, "unit": "events/s",
                        "h2d_bytes_per_step": int(2 * n * net.stride * 4), "d2h_bytes_per_step": int(d2h),
@@ -476,6 +545,13 @@ def main():
         line["cpu_baseline"] = {"value": v, "unit": "events/s", "cores": threads, "kind": "port",
                                 "sample": f"{st} simulation steps after 100 warm-up steps of the same network "
                                           f"({dt:.1f} s), oracle OpenMP port"}
+    if rank == 0 and ws == 1 and not a.no_reference_gpu:
+        line["reference_gpu"] = reference_gpu_leg(cfg)
+        ref_best = line["reference_gpu"].get("best")
+        if ref_best:
+            line["reference_gpu"]["speedup_of_value"] = value / ref_best["events_per_s"]
+    if rank == 0 and ws == 1 and not a.no_large:
+        line["large"] = large_leg(g, a, local)
     if rank == 0 and ws == 1 and not a.no_batched:
         line["batched"] = batched_leg(g, a.batch_networks)
     if rank == 0 and ws == 1 and a.served:
