@@ -69,3 +69,66 @@ def test_protocol_results_feed_the_sweep_summary(g4s, tmp_path):
     assert len({r.spikes for r in runs}) == 1  # every scheme simulates the same network identically
     rows = S.speedup_table(runs, n=500, nsyn=50, modes=(1,))
     assert len(rows) == 6 and all(r[7] > 0 for r in rows)
+
+
+def _g(x) -> str:
+    """A float field as the reference's ofstream writes it: default precision 6, no fixed
+    or scientific flag, i.e. printf's %g of the float's double value (gpu4snn.cu:727-729)."""
+    return "%g" % float(np.float32(x))
+
+
+def _records(st, init: bool) -> bytes:
+    """neuroninfo.csv / neuroninfoafter.csv bytes for a state dict (writeNeuronInfo's field
+    order a b c d v u I id nospks, gpu4snn.cu:727-729; header gpu4snn.cu:1124, 1326)."""
+    n = len(st["a"])
+    out = ["a b c d v u I id nospks\n"]
+    for i in range(n):
+        b = st["b"][i]
+        v, u, I, k = ((-65.0, np.float32(b) * np.float32(-65.0), 0.0, 0) if init
+                      else (st["v"][i], st["u"][i], st["I"][i], int(st["nospks"][i])))
+        out.append(f"{_g(st['a'][i])} {_g(b)} {_g(st['c'][i])} {_g(st['d'][i])} {_g(v)} {_g(u)} {_g(I)} {i} {k}\n")
+    return "".join(out).encode()
+
+
+def test_protocol_result_files_byte_for_byte(g4s, oracle, tmp_path):
+    """g4s_run_protocol's five files per (mode, scheme) against the reference's formats:
+    neuroninfo.csv, spiketimes.csv and neuroninfoafter.csv byte for byte against the same
+    run of the oracle (their content is the exact state and raster); computetime.csv and
+    sim_overview.csv by grammar (their times are measured), with their integer columns
+    against the oracle: headers (gpu4snn.cu:1124, 1134, 1140, 1312), single spaces, the
+    %g floats, one row per neuron / spike / step, and no newline after sim_overview.csv's
+    one row (gpu4snn.cu:1313)."""
+    import re
+    n, nsyn, steps, seed = 500, 100, 200, 5
+    g4s.run_protocol(n, nsyn, steps, algorithm=-1, mode=-1, seed=seed, results_root=str(tmp_path))
+    num = r"-?(?:\d+(?:\.\d*)?|\.\d+)(?:e[+-]\d+)?|inf|nan"
+    for m, scale in enumerate((0.5, 1.0, 1.5)):
+        d = oracle.make_desc(n, nsyn, seed, drive_scale=scale)
+        idx, w = oracle.conn_philox(d)
+        sim = oracle.Sim(d, idx, w)
+        init = sim.state()
+        sim.run(steps)
+        t, i = sim.raster()
+        counts = sim.counts()
+        spikes_txt = ("SpkTime NeuronID\n" + "".join(f"{a} {b}\n" for a, b in zip(t, i))).encode()
+        for alg in range(5):
+            p = tmp_path / "Results" / f"N{n}Nsyn{nsyn}Regime{m}Alg{alg}"
+            assert sorted(x.name for x in p.iterdir()) == ["computetime.csv", "neuroninfo.csv", "neuroninfoafter.csv",
+                                                          "sim_overview.csv", "spiketimes.csv"]
+            assert (p / "neuroninfo.csv").read_bytes() == _records(init, True)
+            assert (p / "spiketimes.csv").read_bytes() == spikes_txt
+            assert (p / "neuroninfoafter.csv").read_bytes() == _records(sim.state(), False)
+            ct = (p / "computetime.csv").read_bytes().decode()
+            lines = ct.split("\n")
+            assert lines[0] == "TimeStep SpksPerStep TimeKernelUpdate TimeSpent" and lines[-1] == ""
+            assert len(lines) == steps + 2
+            for k, row in enumerate(lines[1:-1]):
+                f = row.split(" ")
+                assert len(f) == 4 and f[0] == str(k) and f[1] == str(counts[k])
+                assert all(re.fullmatch(num, x) and _g(float(x)) == x for x in f[2:]), row
+            ov = (p / "sim_overview.csv").read_bytes().decode()
+            head, row = ov.split("\n")
+            assert head == "N elapsed(ms) elapsedwithdata(ms) totalspkcount" and not row.endswith("\n")
+            f = row.split(" ")
+            assert len(f) == 4 and f[0] == str(n) and f[3] == str(len(t))
+            assert all(re.fullmatch(num, x) and ("%g" % float(x)) == x for x in f[1:3]), row
