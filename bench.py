@@ -301,21 +301,57 @@ def served_leg(g, count, lams):
         lat = np.array([r.latency_ms for r in res.values()])
         out[f"lambda_{lam:g}"] = {"req_per_s": count / wall, "events_per_s": st.events / wall,
                                   "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
-                                  "rounds": int(st.rounds), "gpu_busy_ms": st.busy_ms,
+                                  "rounds": int(st.rounds), "gpu_busy_ms": st.busy_ms, "wall_ms": wall * 1e3,
                                   "peak_gib": st.peak_bytes / 2**30, "failed": int(sum(r.status != 0 for r in res.values()))}
+        last = [res[k + 1] for k in range(count)]  # ids are 1.. in submission order
     t0 = time.perf_counter()
-    lat = []
+    lat, alone_ms = [], []
     for k in range(count):
         ts = time.perf_counter()
         with g.Network(int(N[k]), int(S[k]), seed=int(seeds[k]), drive_scale=float(D[k]), record_raster=False) as x:
             x.run(int(T[k]), g.ALG_AUTO)
+            alone_ms.append(x.info().last_run_ms)
         lat.append((time.perf_counter() - ts) * 1e3)
     wall = time.perf_counter() - t0
     out["plain"] = {"req_per_s": count / wall, "p50_service_ms": float(np.percentile(lat, 50)),
-                    "p99_service_ms": float(np.percentile(lat, 99))}
+                    "p99_service_ms": float(np.percentile(lat, 99)), "wall_ms": wall * 1e3,
+                    "device_ms": float(sum(alone_ms)), "host_ms": wall * 1e3 - float(sum(alone_ms))}
     best = max(v["req_per_s"] for k, v in out.items() if k.startswith("lambda_"))
     out["speedup_vs_plain"] = best / out["plain"]["req_per_s"]
+    out["breakdown"] = served_breakdown(N, T, last, np.array(lat), np.array(alone_ms), out["plain"]["wall_ms"])
     return out
+
+
+def served_breakdown(N, T, res, plain_ms, alone_ms, plain_wall_ms, sms=152):
+    """Per-request accounting of the last arrival rate's served run, binned by N x steps:
+    device time alone on the whole GPU (the plain leg, autotuned scheme), device time of
+    the request's steps in the mix and the same times its team's CTAs (SM-ms), creation and
+    queueing.  The bound: the mix cannot finish before its SM time fills every SM, nor
+    before the admission thread has created every network; plain wall / that bound is the
+    best speed-up this mix allows in the batched geometry."""
+    import numpy as np
+    work = N.astype(float) * T
+    edges = [0, 1e7, 1e8, 1e9, np.inf]
+    bins = []
+    for lo, hi in zip(edges[:-1], edges[1:]):
+        m = (work >= lo) & (work < hi)
+        if not m.any():
+            continue
+        sel = [r for r, k in zip(res, m) if k]
+        bins.append({"N_x_steps": f"[{lo:.0e}, {hi:.0e})", "requests": int(m.sum()),
+                     "alone_device_ms": float(alone_ms[m].sum()), "plain_wall_ms": float(plain_ms[m].sum()),
+                     "mix_device_ms": float(sum(r.device_ms for r in sel)),
+                     "mix_sm_ms": float(sum(r.sm_ms for r in sel)),
+                     "mean_team": float(np.mean([r.team for r in sel])),
+                     "create_ms": float(sum(r.create_ms for r in sel)),
+                     "mean_queue_ms": float(np.mean([r.queue_ms for r in sel])),
+                     "mean_latency_ms": float(np.mean([r.latency_ms for r in sel]))})
+    sm_ms = float(sum(r.sm_ms for r in res))
+    create_ms = float(sum(r.create_ms for r in res))
+    longest = float(max(r.device_ms + r.create_ms for r in res))
+    bound = max(sm_ms / sms, create_ms, longest)
+    return {"bins": bins, "sm_ms": sm_ms, "create_ms": create_ms, "longest_request_ms": longest,
+            "bound_ms": bound, "best_speedup_in_this_geometry": plain_wall_ms / bound}
 
 
 def load_traffic(name, steps_per_launch):

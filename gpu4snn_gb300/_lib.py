@@ -79,7 +79,8 @@ class Request(C.Structure):
 class RequestResult(C.Structure):
     _fields_ = [("id", C.c_int64), ("status", C.c_int32), ("steps_done", C.c_int32), ("total_spikes", C.c_int64),
                 ("latency_ms", C.c_double), ("queue_ms", C.c_double), ("rate_hz", C.c_double),
-                ("isi_cv", C.c_double)]
+                ("isi_cv", C.c_double), ("create_ms", C.c_double), ("device_ms", C.c_double),
+                ("sm_ms", C.c_double), ("rounds", C.c_int32), ("team", C.c_int32)]
 
 
 class ServerStats(C.Structure):

@@ -502,6 +502,7 @@ double net_recent_step_ms(const g4s_net *n, int64_t k) {
 const NetView &net_view(const g4s_net *n) { return n->v; }
 cudaStream_t net_stream(const g4s_net *n) { return n->stream; }
 int64_t net_steps_done(const g4s_net *n) { return n->t_abs; }
+int net_team_size(const g4s_net *n) { return n->team_ready && n->team_ok && n->team_p > 0 ? n->team_p : 1; }
 
 }  // namespace g4s
 

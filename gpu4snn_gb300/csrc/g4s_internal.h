@@ -175,6 +175,9 @@ size_t team_smem(int64_t rc, int team);
 const NetView &net_view(const g4s_net *n);
 cudaStream_t net_stream(const g4s_net *n);
 int64_t net_steps_done(const g4s_net *n);
+// CTAs of the team the handle's last planned geometry uses (solo or batched), without
+// planning anything (1 when no team geometry is planned)
+int net_team_size(const g4s_net *n);
 
 // Binary files (g4s_formats.cu): the raster, streamed by a writer thread, and the tables.
 struct RasterFile;

@@ -42,6 +42,10 @@ struct Request {
   int64_t est_bytes = 0;
   int32_t remaining = 0;
   double step_ms = 0.0;  // measured per-step time in the last round (0: not yet run)
+  // accounting of the request's device use: creation, device time of its steps in the
+  // rounds and the same times the CTAs of its team, rounds, last team size
+  double create_ms = 0.0, device_ms = 0.0, sm_ms = 0.0;
+  int32_t rounds = 0, team = 0;
   Clock::time_point t_submit, t_admit, t_done;
   // results, on the host once the request is done
   int status = 0;
@@ -136,6 +140,7 @@ static void admit_loop(g4s_server *s) {
     d.drive_scale = r->req.drive_scale;
     d.record_raster = r->req.record_raster;
     d.raster_budget_bytes = r->req.record_raster ? 4 * r->req.n * (int64_t)s->quantum : 0;
+    const Clock::time_point t_create = Clock::now();
     int rc = g4s_net_create(&d, &r->net);
     // (the team kernel's rows and lists here, off the round thread)
     if (rc == 0 && (rc = net_prepare_rows(r->net)) != 0) {
@@ -143,6 +148,7 @@ static void admit_loop(g4s_server *s) {
       r->net = nullptr;
     }
     r->t_admit = Clock::now();
+    r->create_ms = std::chrono::duration<double, std::milli>(r->t_admit - t_create).count();
     lk.lock();
     if (rc != 0) {
       r->status = rc;
@@ -208,7 +214,13 @@ static void round_loop(g4s_server *s) {
       if (rc != 0) r->status = rc;
       g4s_net_info inf{};
       if (rc == 0 && g4s_net_get_info(r->net, &inf) == 0) ev += inf.last_run_spikes * (int64_t)r->req.nsyn;
-      if (rc == 0 && steps[i] > 0) r->step_ms = net_recent_step_ms(r->net, steps[i]);
+      if (rc == 0 && steps[i] > 0) {
+        r->step_ms = net_recent_step_ms(r->net, steps[i]);
+        r->team = net_team_size(r->net);  // (the batch's team, read without re-planning)
+        r->device_ms += r->step_ms * steps[i];
+        r->sm_ms += r->step_ms * steps[i] * r->team;
+        r->rounds += 1;
+      }
       r->remaining -= steps[i];
       if (r->remaining <= 0 || rc != 0) {
         finish_request(s, r);
@@ -293,6 +305,11 @@ int g4s_server_poll(g4s_server *s, g4s_request_result *out, int32_t cap, int32_t
     o.queue_ms = std::chrono::duration<double, std::milli>(r->t_admit - r->t_submit).count();
     o.rate_hz = r->rate_hz;
     o.isi_cv = r->isi_cv;
+    o.create_ms = r->create_ms;
+    o.device_ms = r->device_ms;
+    o.sm_ms = r->sm_ms;
+    o.rounds = r->rounds;
+    o.team = r->team;
   }
   *n_out = k;
   return G4S_OK;

@@ -21,6 +21,11 @@ class Result:
     queue_ms: float
     rate_hz: float
     isi_cv: float
+    create_ms: float = 0.0  # network creation at admission
+    device_ms: float = 0.0  # device time of its steps in the rounds
+    sm_ms: float = 0.0      # the same times the CTAs of its team
+    rounds: int = 0
+    team: int = 0
 
 
 class Server:
@@ -48,8 +53,8 @@ class Server:
         buf = (_lib.RequestResult * cap)()
         k = C.c_int32()
         check(load().g4s_server_poll(self._h, C.cast(buf, C.c_void_p), cap, C.byref(k)))
-        return [Result(r.id, r.status, r.steps_done, r.total_spikes, r.latency_ms, r.queue_ms, r.rate_hz, r.isi_cv)
-                for r in buf[:k.value]]
+        return [Result(r.id, r.status, r.steps_done, r.total_spikes, r.latency_ms, r.queue_ms, r.rate_hz, r.isi_cv,
+                       r.create_ms, r.device_ms, r.sm_ms, r.rounds, r.team) for r in buf[:k.value]]
 
     def result(self, rid: int) -> dict:
         n = self.sizes[rid]

@@ -234,6 +234,11 @@ typedef struct g4s_request_result {
   double queue_ms;      /* submit -> resident on the device          */
   double rate_hz;       /* FP64 statistics of the run                */
   double isi_cv;
+  double create_ms;     /* network creation at admission (host wall) */
+  double device_ms;     /* device time of its steps in the rounds     */
+  double sm_ms;         /* the same times the CTAs of its team        */
+  int32_t rounds;       /* rounds it took part in                     */
+  int32_t team;         /* CTAs of its team in its last round         */
 } g4s_request_result;
 
 typedef struct g4s_server_stats {
