@@ -90,21 +90,25 @@ def _records(st, init: bool) -> bytes:
     return "".join(out).encode()
 
 
-def test_protocol_result_files_byte_for_byte(g4s, oracle, tmp_path):
+@pytest.mark.parametrize("law", ["philox", "glibc"])
+def test_protocol_result_files_byte_for_byte(g4s, oracle, tmp_path, law):
     """g4s_run_protocol's five files per (mode, scheme) against the reference's formats:
     neuroninfo.csv, spiketimes.csv and neuroninfoafter.csv byte for byte against the same
     run of the oracle (their content is the exact state and raster); computetime.csv and
     sim_overview.csv by grammar (their times are measured), with their integer columns
     against the oracle: headers (gpu4snn.cu:1124, 1134, 1140, 1312), single spaces, the
     %g floats, one row per neuron / spike / step, and no newline after sim_overview.csv's
-    one row (gpu4snn.cu:1313)."""
+    one row (gpu4snn.cu:1313).  Both connectivity laws: the GPU generator's, and the
+    reference's own glibc rand() law (self loops allowed, gpu4snn.cu:873-898)."""
     import re
     n, nsyn, steps, seed = 500, 100, 200, 5
-    g4s.run_protocol(n, nsyn, steps, algorithm=-1, mode=-1, seed=seed, results_root=str(tmp_path))
+    glibc = law == "glibc"
+    g4s.run_protocol(n, nsyn, steps, algorithm=-1, mode=-1, seed=seed, results_root=str(tmp_path),
+                     conn_law=g4s.CONN_GLIBC if glibc else g4s.CONN_PHILOX)
     num = r"-?(?:\d+(?:\.\d*)?|\.\d+)(?:e[+-]\d+)?|inf|nan"
     for m, scale in enumerate((0.5, 1.0, 1.5)):
-        d = oracle.make_desc(n, nsyn, seed, drive_scale=scale)
-        idx, w = oracle.conn_philox(d)
+        d = oracle.make_desc(n, nsyn, seed, drive_scale=scale, self_loops=1 if glibc else 0)
+        idx, w = oracle.conn_glibc(seed, n, nsyn) if glibc else oracle.conn_philox(d)
         sim = oracle.Sim(d, idx, w)
         init = sim.state()
         sim.run(steps)

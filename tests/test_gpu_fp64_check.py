@@ -73,6 +73,7 @@ STATEMENT = {
     (2500, 1000, 1): (67, 2.703e-05, 1.341e-02, 5.177e+01),
     (100_000, 1000, 2): (16, 1.114e-05, 1.081e-03, 4.248e-01),
     (1_000_000, 1000, 3): (14, 1.105e-05, 8.596e-04, 3.589e-01),
+    (250_000, 10_000, 4): (16, 1.103e-05, 1.023e-03, 7.239e-01),
 }
 
 
