@@ -5,8 +5,8 @@ step.  Its currents are exact Q64.64 sums, so it must equal the CPU oracle's FP6
 for bit: per-step max / p99 / median of |v32 - v64| (nearest-rank percentiles), the first
 step whose spike sets differ, and the twin's final v, u.  That is checked at N=2,500 and at
 N=20,000 (a multi-CTA team on the FP32 side).  The same check then states the FP32 error
-against FP64 per configuration (N=2,500, 100,000 and 10^6; Nsyn=1000; the balanced drive;
-200 steps): before the first divergent step the median |dv| stays below 1e-4 mV; the tail
+against FP64 per configuration (N=2,500, 100,000 and 10^6 with Nsyn=1000, N=250,000 with
+Nsyn=10,000; the balanced drive; 200 steps): before the first divergent step the median |dv| stays below 1e-4 mV; the tail
 is carried by neurons on the upswing to threshold, where the half-step map amplifies any
 rounding difference.  Against the FP32 oracle itself the error is zero (the rasters,
 v, u and currents are bit-exact; test_gpu_parity.py, test_gpu_full_size.py).
