@@ -153,5 +153,36 @@ def summary(seeds: int = 10) -> str:
     return "\n".join(lines)
 
 
+def summary_large(steps: int = 100, ap_steps: int = 10) -> str:
+    """The same comparison at N=10^6 x 1000 (the bench's `n1m` network, balanced mode): the
+    reference's five kernels at -O3 (AP for fewer steps: each spike launches a child grid of
+    ceil(N / block) CTAs) and this library's SKL team on the same connectivity."""
+    import sys
+    sys.path.insert(0, os.path.dirname(HERE))
+    from oracle import g4s_oracle as O
+    import gpu4snn_gb300 as g
+
+    n, nsyn, seed = 1_000_000, 1000, 3
+    idx, w = O.conn_philox(O.make_desc(n, nsyn, seed))
+    label = "N=1,000,000 x 1000 (Philox tables, seed 3)"
+    lines = ["| network | scheme | build | steps | spikes | us/step | events/s |", "|---|---|---|---|---|---|---|"]
+    for schemes, st in (((1, 2, 3, 4), steps), ((0,), ap_steps)):
+        for r in run(idx, w, steps=st, schemes=schemes, modes=(1,), seeds=(7,), reps=2):
+            if r["rep"] != 1:
+                continue
+            lines.append(f"| {label} | {SCHEMES[r['scheme']]} (reference, grid {r['grid']} x {r['block']}, "
+                         f"pending-launch limit {r['pending_launch_limit']}) | -O3 | {st} | {r['spikes']} "
+                         f"| {_fmt(r['ms'] * 1e3 / st, 2)} | {r['spikes'] * nsyn / (r['ms'] * 1e-3):.3e} |")
+    del idx, w
+    with g.Network(n, nsyn, seed=seed, record_raster=False) as net:
+        net.run(1000, 4)
+        net.run(1000, 4)
+        inf = net.info()
+        lines.append(f"| {label} | SKL (this library) | -O3 | 1000 | {inf.last_run_spikes} "
+                     f"| {_fmt(inf.last_run_ms, 2)} | {inf.last_run_spikes * nsyn / (inf.last_run_ms * 1e-3):.3e} |")
+    return "\n".join(lines)
+
+
 if __name__ == "__main__":
-    print(summary())
+    import sys
+    print(summary_large() if sys.argv[1:] == ["large"] else summary())
