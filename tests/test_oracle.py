@@ -197,3 +197,22 @@ def test_rate_and_isi_agree_fp32_fp64_full_run(oracle):
     a, b = s32.stats(), s64.stats()
     assert abs(a.rate_hz - b.rate_hz) / b.rate_hz < 0.01
     assert abs(a.isi_cv - b.isi_cv) / b.isi_cv < 0.01
+
+
+def test_sort_rows_matches_numpy_order(oracle):
+    """The oracle's parallel radix row sort puts every row in the library's order: target as
+    unsigned (so padding, -1, last), equal targets by weight bits; generated rows (distinct
+    targets, padded stride) and rows with repeated targets and negative weights alike."""
+    rng = np.random.default_rng(3)
+    d = oracle.make_desc(700, 37, 9)  # stride 40: three padding slots a row
+    idx, w = oracle.conn_philox(d)
+    rep_i = rng.integers(0, 50, size=(300, 64)).astype(np.int32)
+    rep_i[:, -5:] = -1
+    rep_w = rng.standard_normal((300, 64)).astype(np.float32)
+    for ti, tw in ((idx, w), (rep_i, rep_w)):
+        key = (ti.view(np.uint32).astype(np.uint64) << np.uint64(32)) | tw.view(np.uint32).astype(np.uint64)
+        order = np.argsort(key, axis=1, kind="stable")
+        want_i, want_w = np.take_along_axis(ti, order, 1), np.take_along_axis(tw, order, 1)
+        gi, gw = ti.copy(), tw.copy()
+        oracle.sort_rows(gi, gw)
+        assert np.array_equal(gi, want_i) and np.array_equal(gw.view(np.uint32), want_w.view(np.uint32))
