@@ -221,6 +221,9 @@ struct g4s_net {
   unsigned long long *list = nullptr;
   uint16_t *seg = nullptr;
   size_t seg_bytes = 0;
+  // device memory from this stream-ordered pool (a server's, which keeps freed memory for
+  // the next requests' networks), allocated and freed on the handle's stream; null: cudaMalloc
+  cudaMemPool_t pool = nullptr;
   int want_p = 0;
   int deliver_mode = kDeliverRun;
   int team_nt = 0;            // threads per CTA asked for: kTeamNT, kTeamNTSmall, 0 = automatic
@@ -237,6 +240,18 @@ struct g4s_net {
 
 static std::atomic<int> g_fail_next_alloc{0};
 
+static cudaError_t net_malloc(g4s_net *n, void **p, size_t bytes) {
+  if (n->pool) return cudaMallocFromPoolAsync(p, bytes, n->pool, n->stream);
+  return cudaMalloc(p, bytes);
+}
+static void net_free(g4s_net *n, const void *p) {
+  if (!p) return;
+  if (n->pool)
+    cudaFreeAsync(const_cast<void *>(p), n->stream);
+  else
+    cudaFree(const_cast<void *>(p));
+}
+
 static void free_net(g4s_net *n) {
   if (!n) return;
   NetView &v = n->v;
@@ -248,26 +263,26 @@ static void free_net(g4s_net *n) {
   for (auto &gr : n->step_graphs)  // (and so do the captured chunks)
     if (gr.exec) cudaGraphExecDestroy(gr.exec);
   n->step_graphs.clear();
-  cudaFree(n->d_t0);
+  net_free(n, n->d_t0);
   cudaFreeHost(n->h_t0);
-  cudaFree(const_cast<int2 *>(v.pair));
-  cudaFree(v.vu);
-  cudaFree(v.abcd);
-  cudaFree(v.rpar);
-  cudaFree(v.acc);
-  cudaFree(v.ilast);
-  cudaFree(v.sstat);
-  cudaFree(const_cast<int *>(v.idx));
-  cudaFree(const_cast<float *>(v.w));
-  cudaFree(v.raster);
-  cudaFree(v.counts);
-  cudaFree(v.base);
-  cudaFree(v.stamps);
-  cudaFree(v.status);
-  cudaFree(n->gs);
-  cudaFree(n->d_stats);
-  cudaFree(n->seg);
-  cudaFree(n->list);
+  net_free(n, const_cast<int2 *>(v.pair));
+  net_free(n, v.vu);
+  net_free(n, v.abcd);
+  net_free(n, v.rpar);
+  net_free(n, v.acc);
+  net_free(n, v.ilast);
+  net_free(n, v.sstat);
+  net_free(n, const_cast<int *>(v.idx));
+  net_free(n, const_cast<float *>(v.w));
+  net_free(n, v.raster);
+  net_free(n, v.counts);
+  net_free(n, v.base);
+  net_free(n, v.stamps);
+  net_free(n, v.status);
+  net_free(n, n->gs);
+  net_free(n, n->d_stats);
+  net_free(n, n->seg);
+  net_free(n, n->list);
   cudaFreeHost(n->h_counts);
   cudaFreeHost(n->h_base);
   cudaFreeHost(n->h_stamps);
@@ -301,7 +316,7 @@ static int validate(const g4s_net_desc *d) {
 template <class T>
 static int dalloc(g4s_net *n, T **p, size_t count, const char *what) {
   const size_t bytes = count * sizeof(T);
-  cudaError_t e = g_fail_next_alloc.exchange(0) ? cudaErrorMemoryAllocation : cudaMalloc((void **)p, bytes ? bytes : 16);
+  cudaError_t e = g_fail_next_alloc.exchange(0) ? cudaErrorMemoryAllocation : net_malloc(n, (void **)p, bytes ? bytes : 16);
   if (e != cudaSuccess) {
     *p = nullptr;
     return set_error(G4S_ERR_NOMEM, std::string("cudaMalloc of ") + what + " (" + std::to_string(bytes) +
@@ -316,11 +331,12 @@ static void set_drive(g4s_net *n) {
   n->v.gi = 2.0f * n->desc.drive_scale;
 }
 
-static int alloc_net(const g4s_net_desc *d, g4s_net **out) {
+static int alloc_net(const g4s_net_desc *d, g4s_net **out, cudaMemPool_t pool = nullptr) {
   int rc = validate(d);
   if (rc) return rc;
   g4s_net *n = new (std::nothrow) g4s_net;
   if (!n) return set_error(G4S_ERR_NOMEM, "host allocation");
+  n->pool = pool;
   static std::atomic<uint64_t> next_serial{1};
   n->serial = next_serial++;
   n->desc = *d;
@@ -351,6 +367,18 @@ static int alloc_net(const g4s_net_desc *d, g4s_net **out) {
     free_net(n);
     return cuda_error(e, "cudaMemGetInfo");
   }
+  if (pool) {  // memory the pool holds for reuse counts as free
+    uint64_t reserved = 0, used = 0;
+    if (cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReservedMemCurrent, &reserved) == cudaSuccess &&
+        cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemCurrent, &used) == cudaSuccess && reserved > used)
+      free_b += (size_t)(reserved - used);
+    (void)cudaGetLastError();
+    // (a pool allocates on the handle's stream)
+    if ((e = cudaStreamCreateWithFlags(&n->stream, cudaStreamNonBlocking)) != cudaSuccess) {
+      free_net(n);
+      return cuda_error(e, "stream");
+    }
+  }
   const size_t need = N * S * 8 + N * (8 + 16 + 4 + 8 + 4 + 32) + (size_t)v.raster_cap * 4 + (size_t)cs * 32;
   if (need + ((size_t)256 << 20) > free_b) {
     free_net(n);
@@ -371,7 +399,7 @@ static int alloc_net(const g4s_net_desc *d, g4s_net **out) {
     free_net(n);
     return rc;
   }
-  if ((e = cudaStreamCreateWithFlags(&n->stream, cudaStreamNonBlocking)) != cudaSuccess ||
+  if ((!n->stream && (e = cudaStreamCreateWithFlags(&n->stream, cudaStreamNonBlocking)) != cudaSuccess) ||
       (e = cudaEventCreate(&n->ev0)) != cudaSuccess || (e = cudaEventCreate(&n->ev1)) != cudaSuccess ||
       (e = cudaEventCreate(&n->ek0)) != cudaSuccess || (e = cudaEventCreate(&n->ek1)) != cudaSuccess ||
       (e = cudaMallocHost((void **)&n->h_counts, (size_t)cs * 4)) != cudaSuccess ||
@@ -606,7 +634,7 @@ static bool plan_team(g4s_net *n, int want, bool batch, int64_t slice, int *p_ou
 static int prepare_rows(g4s_net *n) {
   if (!n->v.pair) {
     const size_t bytes = (size_t)n->v.n * (size_t)n->v.stride * sizeof(int2);
-    if (!g_fail_next_alloc.exchange(0) && cudaMalloc((void **)&n->v.pair, bytes) == cudaSuccess) {
+    if (!g_fail_next_alloc.exchange(0) && net_malloc(n, (void **)&n->v.pair, bytes) == cudaSuccess) {
       n->device_bytes += bytes;
       n->pair_ready = false;
     } else {
@@ -620,7 +648,7 @@ static int prepare_rows(g4s_net *n) {
     n->pair_ready = true;
   }
   if (!n->list) {
-    cudaError_t e = cudaMalloc((void **)&n->list, (size_t)n->v.n * 4 * sizeof(unsigned long long));
+    cudaError_t e = net_malloc(n, (void **)&n->list, (size_t)n->v.n * 4 * sizeof(unsigned long long));
     if (e != cudaSuccess) return cuda_error(e, "spike lists");
     G4S_CUDA(cudaMemsetAsync(n->list, 0, (size_t)n->v.n * 4 * sizeof(unsigned long long), n->stream));
     G4S_CUDA(cudaStreamSynchronize(n->stream));
@@ -657,11 +685,11 @@ static int prepare_team(g4s_net *n, bool batch = false, int64_t slice = kBatchSl
   if (p > 1) {
     const size_t bytes = (size_t)n->v.n * (size_t)(p + 1) * sizeof(uint16_t);
     if (bytes > n->seg_bytes) {
-      cudaFree(n->seg);
+      net_free(n, n->seg);
       n->seg = nullptr;
       n->device_bytes -= n->seg_bytes;
       n->seg_bytes = 0;
-      cudaError_t e = cudaMalloc((void **)&n->seg, bytes);
+      cudaError_t e = net_malloc(n, (void **)&n->seg, bytes);
       if (e != cudaSuccess) return cuda_error(e, "segment table");
       n->seg_bytes = bytes;
       n->device_bytes += bytes;
@@ -1475,11 +1503,11 @@ int g4s_set_device(int32_t device) {
   return G4S_OK;
 }
 
-int g4s_net_create(const g4s_net_desc *desc, g4s_net **out) {
+static int create_net(const g4s_net_desc *desc, cudaMemPool_t pool, g4s_net **out) {
   if (!out) return set_error(G4S_ERR_INVALID, "null output handle");
   *out = nullptr;
   g4s_net *n = nullptr;
-  int rc = alloc_net(desc, &n);
+  int rc = alloc_net(desc, &n, pool);
   if (rc) return rc;
   if (desc->conn_law == G4S_CONN_GLIBC) {
     const size_t cnt = (size_t)n->v.n * (size_t)n->v.stride;
@@ -1508,6 +1536,8 @@ int g4s_net_create(const g4s_net_desc *desc, g4s_net **out) {
   *out = n;
   return G4S_OK;
 }
+
+int g4s_net_create(const g4s_net_desc *desc, g4s_net **out) { return create_net(desc, nullptr, out); }
 
 int g4s_net_create_from_tables(const g4s_net_desc *desc, const int32_t *idx, const float *w, int32_t stride,
                                g4s_net **out) {
@@ -1923,3 +1953,9 @@ int g4s_net_create_from_file(const g4s_net_desc *desc, const char *path, g4s_net
 }
 
 }  // extern "C"
+
+namespace g4s {
+int net_create_pooled(const g4s_net_desc *desc, cudaMemPool_t pool, g4s_net **out) {
+  return create_net(desc, pool, out);
+}
+}  // namespace g4s

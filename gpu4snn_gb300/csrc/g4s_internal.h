@@ -9,6 +9,7 @@
 #include "g4s_types.h"
 
 struct g4s_net;  // the handle of the C ABI
+struct g4s_net_desc;
 
 namespace g4s {
 
@@ -166,6 +167,8 @@ double net_recent_step_ms(const g4s_net *n, int64_t k);
 // the team kernel's team-independent buffers of a handle (its interleaved rows and spike
 // lists), made ready ahead of its first team run; nothing for tables the kernel cannot run
 int net_prepare_rows(g4s_net *n);
+// g4s_net_create with the handle's device memory from a stream-ordered pool (a server's)
+int net_create_pooled(const g4s_net_desc *desc, cudaMemPool_t pool, g4s_net **out);
 cudaError_t team_smem_ceiling();  // the part of team_max_blocks that launch_team needs
 // shared memory of one rank of a team of `team` CTAs with `rc` neurons each (0: does not fit)
 size_t team_smem(int64_t rc, int team);

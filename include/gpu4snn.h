@@ -214,8 +214,9 @@ int g4s_run_protocol(int32_t n, int32_t nsyn, int32_t iterations, int32_t algori
  * `quantum_steps` steps in a request's first round, then as many as the median resident
  * request runs in `quantum_steps` steps, from the measured per-step times (at most
  * `quantum_steps` for a request that records its raster); requests arriving meanwhile
- * join at the next round.  submit/poll/
- * result/release/get_stats are thread-safe. */
+ * join at the next round.  The requests' device memory comes from a pool of the server's
+ * that keeps what finished requests free for the next ones: the server holds its peak
+ * device memory until it stops.  submit/poll/result/release/get_stats are thread-safe. */
 typedef struct g4s_request {
   int64_t n;           /* neurons                                   */
   int32_t nsyn;        /* synapses per neuron                       */

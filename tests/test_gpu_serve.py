@@ -95,6 +95,25 @@ def test_server_budget_and_rejections(g4s):
         assert srv.stats().peak_bytes <= 200 << 20
 
 
+def test_server_stop_without_drain(g4s):
+    """Stopping with requests queued, resident and finishing: the resident ones finish,
+    the retire thread frees every finished network, the queued ones are dropped, and the
+    call returns; a second server then runs normally."""
+    from gpu4snn_gb300.server import Server
+    srv = Server(hbm_budget_bytes=300 << 20, quantum=40)
+    for k in range(8):
+        srv.submit(15000 + 1000 * k, 300, 60 + 20 * k, 300 + k, 1.0)
+    time.sleep(0.05)
+    done_before = len(srv.poll())
+    t0 = time.time()
+    srv.stop(drain=False)
+    assert time.time() - t0 < 120.0 and done_before <= 8
+    with Server(hbm_budget_bytes=300 << 20, quantum=40) as srv2:
+        rid = srv2.submit(8000, 200, 50, 7, 1.0)
+        res = _wait_all(srv2, 1)
+        assert res[rid].status == 0 and res[rid].steps_done == 50
+
+
 def test_autotune_does_not_perturb(g4s, oracle):
     n, nsyn, seed = 20000, 300, 7
     d = oracle.make_desc(n, nsyn, seed)
