@@ -426,10 +426,12 @@ def timed_leg(g, net, name, cfg, alg, a, pg, local, drive_override):
             "last_alg": last_alg, "roofline": roofline, "clocks": clk.summary()}
 
 
-def large_leg(g, a, local):
+def large_leg(g, a, local, drives=(0.5, 2.0)):
     """The large single networks at their workloads' own drive, each on its own: N=10^6 x
     1000 and N=250,000 x 10,000, SKL (the autotuner's pick for both), with the roofline of
-    that launch, its clocks and its DRAM traffic from the committed ncu summary."""
+    that launch, its clocks and its DRAM traffic from the committed ncu summary; then the
+    same networks at the other drive scales of the sweep (the quiet and the irregular
+    regime), each a fresh network timed the same way."""
     out = {}
     for name in ("n1m", "n250k_s10k"):
         cfg = WORKLOADS[name]
@@ -444,6 +446,19 @@ def large_leg(g, a, local):
                      "steps": a.steps, "warmup": a.warmup, "firing_rate_hz": r["spikes"] / (n * T * a.steps) * 1e3,
                      "config": workload_config(name, cfg), "create_s": create_s, "roofline": r["roofline"],
                      "clocks": r["clocks"], "gpu_launches": int(r["launches"])}
+        sweep = {}
+        for d in drives:
+            dcfg = (n, nsyn, T, d, seed)
+            net = g.Network(n, nsyn, seed=seed, drive_scale=d, record_raster=False)
+            r = timed_leg(g, net, name, dcfg, g.ALG_SKL, a, None, local, True)
+            net.close()
+            sweep[f"drive_{d:g}"] = {"value": r["events"] / (r["dev_ms"] * 1e-3), "unit": "events/s",
+                                     "us_per_sim_step": r["dev_ms"] * 1e3 / (a.steps * T),
+                                     "firing_rate_hz": r["spikes"] / (n * T * a.steps) * 1e3,
+                                     "frac": r["roofline"]["frac"],
+                                     "delivery_frac": r["roofline"]["delivery_phase"]["frac"],
+                                     "kernel": r["roofline"]["kernel"], "clocks": r["clocks"]}
+        out[name]["drive_sweep"] = sweep
     return out
 
 
