@@ -113,6 +113,7 @@ SIGNATURES = [
     ("g4s_net_set_block_threads", C.c_int, [_P, C.c_int32]),
     ("g4s_net_get_block_threads", C.c_int, [_P, C.POINTER(C.c_int32)]),
     ("g4s_net_get_geometry", C.c_int, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int64)]),
+    ("g4s_net_get_delivery", C.c_int, [_P, C.POINTER(C.c_int32)]),
     ("g4s_nets_run", C.c_int, [_P, _P, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_int64)]),
     ("g4s_net_autotune", C.c_int, [_P, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                    C.POINTER(C.c_double)]),

@@ -162,7 +162,7 @@ struct TeamLaunch {
 struct TuneChoice {
   int alg = kAlgSKL;
   int team = 0;
-  int mode = kDeliverRun;
+  int mode = kDeliverAuto;
   int nt = 0;  // threads per CTA of the team kernel (0: chosen from the step size)
 };
 
@@ -225,7 +225,7 @@ struct g4s_net {
   // the next requests' networks), allocated and freed on the handle's stream; null: cudaMalloc
   cudaMemPool_t pool = nullptr;
   int want_p = 0;
-  int deliver_mode = kDeliverRun;
+  int deliver_mode = kDeliverAuto;
   int team_nt = 0;            // threads per CTA asked for: kTeamNT, kTeamNTSmall, 0 = automatic
   int team_nt_eff = kTeamNT;  // ... in use (set when the team is planned)
   bool tables_fit = false;
@@ -892,6 +892,13 @@ static int absorb_chunk(g4s_net *n, int cs, int64_t *spikes) {
 // it and checks every network's status words.  Between the two, the host may work on the
 // previous round's results, but must not touch the pinned per-step buffers (the round's
 // graph writes them at its end) nor the networks' device arrays.
+// Delivery mapping of a network's multi-CTA team: the one set or tuned, else eight-lane
+// groups when a rank's segment of a row holds kGroupMinSegment synapses or more on average.
+static int deliver_mode_of(const g4s_net *n) {
+  if (n->deliver_mode != kDeliverAuto) return n->deliver_mode;
+  return n->team_p > 1 && (int64_t)n->v.nsyn >= (int64_t)kGroupMinSegment * n->team_p ? kDeliverGroup : kDeliverRun;
+}
+
 static int team_round_start(g4s_net *const *nets, const int *steps, const bool *last, int count, TeamLaunch &L,
                             cudaStream_t s, unsigned long long limit_ns, int stall) {
   std::vector<int> order;
@@ -938,7 +945,7 @@ static int team_round_start(g4s_net *const *nets, const int *steps, const bool *
     it.team = n->team_p;
     it.rc = (int)n->team_rc;
     it.sync = n->gs;
-    it.mode = n->deliver_mode;
+    it.mode = deliver_mode_of(n);
     it.cap = team_window(n->team_rc, n->team_p);
     if ((uint64_t)n->tag_next + (uint64_t)steps[i] + 2 >= 0xFFFFFFFFull) {  // tags would wrap: start over
       G4S_CUDA(cudaMemsetAsync(n->list, 0, (size_t)n->v.n * 4 * sizeof(unsigned long long), s));
@@ -1377,11 +1384,16 @@ static int autotune(g4s_net *n, int32_t probe, TuneChoice *best, double *best_us
   std::vector<int> teams = {0};
   for (int p = 1; p <= pmax; p *= 2) teams.push_back(p);
   if (pmax > 1) teams.push_back(pmax);
-  // segment-run delivery only: lane-per-spike measured slower or equal on every
-  // configuration tried (it stays available through g4s_net_set_geometry)
-  // each team size with both CTA sizes of the team kernel
+  // each team size with both CTA sizes of the team kernel, by segment runs and, where a
+  // rank's segment of a row averages half the automatic threshold or more, by eight-lane
+  // groups too
   for (int p : teams)
-    for (int nt : {kTeamNT, kTeamNTSmall}) cand.push_back(TuneChoice{kAlgSKL, p, kDeliverRun, nt});
+    for (int nt : {kTeamNT, kTeamNTSmall}) {
+      cand.push_back(TuneChoice{kAlgSKL, p, kDeliverRun, nt});
+      const int pe = p == 0 ? pmax : p;
+      if (pe > 1 && 2 * (int64_t)n->v.nsyn >= (int64_t)kGroupMinSegment * pe)
+        cand.push_back(TuneChoice{kAlgSKL, p, kDeliverGroup, nt});
+    }
   cand.push_back(TuneChoice{kAlgAB, 0, kDeliverRun});
   cand.push_back(TuneChoice{kAlgAP, 0, kDeliverRun});
   const int keep_mode = n->deliver_mode, keep_nt = n->team_nt;
@@ -1602,8 +1614,9 @@ int g4s_net_load_tables(g4s_net *n, const int32_t *idx, const float *w, int32_t 
 int g4s_net_set_geometry(g4s_net *n, int32_t owner_blocks, int32_t delivery) {
   if (!n) return set_error(G4S_ERR_INVALID, "null handle");
   if (owner_blocks < 0) return set_error(G4S_ERR_INVALID, "owner_blocks must be >= 0 (0 = automatic)");
-  if (delivery != kDeliverRun && delivery != kDeliverLane)
-    return set_error(G4S_ERR_INVALID, "delivery must be 0 (segment runs) or 1 (lane per spike)");
+  if (delivery != kDeliverAuto && delivery != kDeliverRun && delivery != kDeliverGroup)
+    return set_error(G4S_ERR_INVALID,
+                     "delivery must be -1 (automatic), 0 (segment runs) or 1 (eight lanes a spike)");
   n->want_p = owner_blocks;
   n->deliver_mode = delivery;
   n->team_ready = false;
@@ -1636,6 +1649,14 @@ int g4s_net_get_geometry(g4s_net *n, int32_t *owner_blocks, int64_t *slice) {
   const bool ok = n->team_ok && n->team_ready;
   if (owner_blocks) *owner_blocks = ok ? n->team_p : 0;
   if (slice) *slice = ok ? n->team_rc : 0;
+  return G4S_OK;
+}
+
+int g4s_net_get_delivery(g4s_net *n, int32_t *delivery) {
+  if (!n || !delivery) return set_error(G4S_ERR_INVALID, "null argument");
+  const int rc = prepare_team(n);
+  if (rc) return rc;
+  *delivery = n->team_ok && n->team_ready && n->team_p > 1 ? deliver_mode_of(n) : kDeliverAuto;
   return G4S_OK;
 }
 

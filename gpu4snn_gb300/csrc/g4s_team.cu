@@ -41,19 +41,20 @@
 //   delivery  one-CTA team: whole spiking rows, 128-bit loads, flat over all threads.
 //             Larger team: every rank reads, for every spike, the segment of the spiking
 //             row whose targets fall in its slice (rows are sorted by target and a per-row
-//             offset table gives the segment).  The run and lane mappings read the rows
+//             offset table gives the segment).  The run and group mappings read the rows
 //             interleaved as (target, weight bits) pairs, so a segment of ~7 synapses is one
 //             contiguous run of sectors instead of two half-used ones: at 7,000 spikes per
-//             step this cut the delivery by a third (the step is bound by the sectors in
-//             flight per SM, not by the bytes).  Flat mapping (at least kFlatMinSpikes
+//             step this cut the delivery by a third.  Flat mapping (at least kFlatMinSpikes
 //             staged spikes, at most kFlatMax synapses for the rank, and, in a 768-thread
 //             CTA, fewer than NT/2 spikes): the segment bounds
 //             of all spikes at once, a block scan, every synapse of the concatenation
 //             mapped to its spike in shared memory, and thread i walks synapses i, i+NT,
 //             ... with eight reads in flight.  Run mapping (otherwise): a warp takes 32
 //             spikes, scans their segment lengths and walks the concatenated segments,
-//             eight synapses per lane in flight.  Each weight goes into the rank's own
-//             shared memory.
+//             eight synapses per lane in flight, each lane finding its synapse's spike by
+//             a shuffle search.  Group mapping (the team's choice for long segments): the
+//             warp's 32 spikes in 8 rounds of 4, eight lanes walking each spike's segment,
+//             no search.  Each weight goes into the rank's own shared memory.
 //   tail      the raster and the spike statistics of this rank's spikes, and the next
 //             step's drive, handed out in chunks of 32 neurons to warps as they finish
 //             delivering (the flat mapping computes each thread's own neuron's drive
@@ -775,47 +776,54 @@ __device__ void team_run(const TeamItem &it, int rank, unsigned char *s_raw, Tea
             if (t[u] >= 0) acc_add(base_a, base_b, (unsigned)(t[u] - (int)lo), wfix(w[u]));
         }
         zdone = zwant ? min(cnt, NT) : 0;
-      } else if (it.mode == kDeliverLane) {
-        // ---- delivery, larger team, one lane per spike: each lane walks its own segment,
-        // four synapses (eight loads) at a time; the warp's next 32 spike ids and segment
-        // bounds are loaded while the current ones are walked.  No shuffles: the shared-
-        // memory pipe carries only the atomics.
+      } else if (it.mode == kDeliverGroup) {
+        // ---- delivery, larger team, eight lanes a spike (long segments): warps take the
+        // step's spikes in batches of 32 as in the run mapping (`wpb` warps sharing a batch's
+        // rounds when there are fewer batches than warps); a batch is walked in 8 rounds of 4
+        // spikes, lane group g (lanes 8g .. 8g+7) reading spike 4r+g's segment in contiguous
+        // 32-synapse steps, four reads a lane in flight.  No search: a segment's synapses
+        // need no shuffles to find their spike.  The next batch's ids and bounds are loaded
+        // while the current one is walked.
         const uint64_t pkeep = policy_evict_last();
-        int q = warp * 32 + lane;
+        const int nbatch = (Kw + 31) >> 5;
+        const int wpb = nbatch >= kWarps ? 1 : min(8, kWarps / max(nbatch, 1));
+        const int groups = kWarps / wpb, gw = warp / wpb, wi = warp % wpb;
+        const int sub = lane & 7, grp = lane >> 3;
         int s = 0, b = 0, e = 0;
-        if (q < Kw) {
-          s = gl ? tagged_id(dense + q, tag, sh, it.sync, lim) : list[q];
-          const uint16_t *so = it.seg + (size_t)s * segw + rank;
-          b = ld_keep_u16(so, pkeep);
-          e = ld_keep_u16(so + 1, pkeep);
-        }
-        for (int q0 = warp * 32; q0 < Kw; q0 += kWarps * 32) {
-          const long long row = (long long)s * v.stride;
-          const int cb = b, ce = e;
-          q = q0 + kWarps * 32 + lane;
+        auto fetch = [&](int batch) {
+          const int q = batch * 32 + lane;
           s = 0;
           b = 0;
           e = 0;
-          if (q < Kw) {
+          if (gw < groups && batch < nbatch && q < Kw) {
             s = gl ? tagged_id(dense + q, tag, sh, it.sync, lim) : list[q];
             const uint16_t *so = it.seg + (size_t)s * segw + rank;
             b = ld_keep_u16(so, pkeep);
             e = ld_keep_u16(so + 1, pkeep);
           }
-          for (int j = cb; j < ce; j += 4) {
-            int t[4];
-            float w[4];
+        };
+        fetch(gw);
+        for (int batch = gw; gw < groups && batch < nbatch; batch += groups) {
+          const long long rowb = (long long)s * v.stride + b;  // segment start of this lane's spike
+          const int len = e - b;
+          fetch(batch + groups);  // next batch, in flight meanwhile
+          for (int r = wi; r < 8; r += wpb) {
+            const long long rb = __shfl_sync(0xFFFFFFFFu, rowb, r * 4 + grp);
+            const int ln = __shfl_sync(0xFFFFFFFFu, len, r * 4 + grp);
+            for (int k0 = 0; k0 < ln; k0 += 32) {
+              int t[4];
+              float w[4];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
-              t[u] = -1;
-              w[u] = 0.0f;
-              if (j + u < ce) {
-                synapse(row + j + u, t[u], w[u]);
+              for (int u = 0; u < 4; ++u) {
+                const int k = k0 + u * 8 + sub;
+                t[u] = -1;
+                w[u] = 0.0f;
+                if (k < ln) synapse(rb + k, t[u], w[u]);
               }
-            }
 #pragma unroll
-            for (int u = 0; u < 4; ++u)
-              if (t[u] >= 0) acc_add(base_a, base_b, (unsigned)(t[u] - (int)lo), wfix(w[u]));
+              for (int u = 0; u < 4; ++u)
+                if (t[u] >= 0) acc_add(base_a, base_b, (unsigned)(t[u] - (int)lo), wfix(w[u]));
+            }
           }
         }
       } else {

@@ -73,14 +73,20 @@ struct TeamItem {
   int team;             // CTAs of the team
   int rc;               // neurons per CTA slice
   GridSync *sync;       // error word of the team
-  int mode;             // delivery mapping of a multi-CTA team (kDeliverRun or kDeliverLane)
+  int mode;             // delivery mapping of a multi-CTA team (kDeliverRun or kDeliverGroup)
   int cap;              // delivery window of a multi-CTA rank (spike ids in shared memory)
   unsigned tag0;        // record tag of step lt: tag0 + lt + 1 (never repeats for the list's words)
 };
 
 // Delivery mappings of a multi-CTA team: warps walk the concatenated segments of 32
-// spikes (kDeliverRun), or each lane walks one spike's segment (kDeliverLane).
+// spikes, each synapse finding its spike by a search over the batch (kDeliverRun, for
+// short segments), or groups of eight lanes walk one spike's segment each (kDeliverGroup,
+// for long segments: no search); kDeliverAuto picks by the mean segment length.
+constexpr int kDeliverAuto = -1;
 constexpr int kDeliverRun = 0;
-constexpr int kDeliverLane = 1;
+constexpr int kDeliverGroup = 1;
+// mean synapses of a rank's segment of a row (Nsyn / team) from which kDeliverAuto takes the
+// eight-lane groups (measured: ~20 synapses even, 53 and 66 a quarter faster than the runs)
+constexpr int kGroupMinSegment = 24;
 
 }  // namespace g4s

@@ -89,8 +89,9 @@ class Network:
     def inject_fault(self, kind: int):
         check(load().g4s_inject_fault(self._h, kind))
 
-    def set_geometry(self, owner_blocks: int = 0, delivery: int = 0):
-        """SKL owner CTAs (0 = automatic) and delivery mapping (0 segment runs, 1 lane per spike)."""
+    def set_geometry(self, owner_blocks: int = 0, delivery: int = -1):
+        """SKL owner CTAs (0 = automatic) and delivery mapping of a multi-CTA team (-1
+        automatic, 0 segment runs, 1 eight lanes a spike)."""
         check(load().g4s_net_set_geometry(self._h, owner_blocks, delivery))
 
     def set_block_threads(self, threads: int):
@@ -115,6 +116,13 @@ class Network:
         p, rc = C.c_int32(), C.c_int64()
         check(load().g4s_net_get_geometry(self._h, C.byref(p), C.byref(rc)))
         return p.value, rc.value
+
+    def delivery(self) -> int:
+        """Delivery mapping in use: 0 segment runs, 1 eight lanes a spike, -1 without a
+        multi-CTA team."""
+        d = C.c_int32()
+        check(load().g4s_net_get_delivery(self._h, C.byref(d)))
+        return d.value
 
     def load_tables(self, idx: np.ndarray, w: np.ndarray):
         idx = np.ascontiguousarray(idx, dtype=np.int32)

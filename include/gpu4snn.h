@@ -132,11 +132,13 @@ int g4s_net_set_barrier_timeout(g4s_net *net, uint64_t ns);
 /* Geometry of the SKL kernel (the reference sizes its persistent grids from occupancy,
  * gpu4snn.cu:1066-1076): `owner_blocks` CTAs, each owning a contiguous slice of target
  * neurons whose currents stay in its shared memory (0 = automatic), and the delivery
- * mapping of a multi-CTA team (0: warps walk the concatenated segments of 32 spikes;
- * 1: one lane per spike).  get_geometry reports the geometry in use (zeros when the
- * network is too large for shared-memory ownership, or its tables exceed the
- * exact-accumulation bound, and the global-atomic persistent kernel runs instead) and the
- * neurons per CTA. */
+ * mapping of a multi-CTA team (-1, the default: automatic, eight-lane groups when a rank's
+ * segment of a row averages 24 synapses or more, else segment runs; 0: warps walk the
+ * concatenated segments of 32 spikes; 1: eight lanes walk each spike's segment).
+ * get_geometry reports the geometry in use (zeros when the network is too large for
+ * shared-memory ownership, or its tables exceed the exact-accumulation bound, and the
+ * global-atomic persistent kernel runs instead) and the neurons per CTA; get_delivery the
+ * mapping in use (0 or 1; -1 without a multi-CTA team).  Results do not depend on either. */
 int g4s_net_set_geometry(g4s_net *net, int32_t owner_blocks, int32_t delivery);
 /* Threads per CTA of the SKL team kernel: 1024 (the most table reads in flight, for steps
  * with many synapses per CTA), 768 (80 registers a thread instead of 64, no spills: faster
@@ -147,6 +149,7 @@ int g4s_net_set_geometry(g4s_net *net, int32_t owner_blocks, int32_t delivery);
 int g4s_net_set_block_threads(g4s_net *net, int32_t threads);
 int g4s_net_get_block_threads(g4s_net *net, int32_t *threads);
 int g4s_net_get_geometry(g4s_net *net, int32_t *owner_blocks, int64_t *slice);
+int g4s_net_get_delivery(g4s_net *net, int32_t *delivery);
 
 /* Autotuner (replaces the reference's occupancy-based launch configurator,
  * gpu4snn.cu:780-838, 959-1079): times the candidate schemes (SKL with teams of 1, 2, 4, ...

@@ -217,11 +217,32 @@ def test_owner_geometries(g4s, oracle, p, n, mode):
         compare_state(net, sim)
 
 
+@pytest.mark.parametrize("n,nsyn,p,want", [(20_000, 4000, 0, 1), (20_000, 1000, 0, 0), (30_000, 600, 16, 1),
+                                           (30_000, 600, 32, 0)])
+def test_automatic_delivery_mapping(g4s, oracle, n, nsyn, p, want):
+    """Untouched, a multi-CTA team delivers by eight-lane groups when a rank's segment of a
+    row averages 24 synapses or more (Nsyn / team), else by segment runs; either way the
+    raster, state and pending currents equal the oracle's."""
+    seed = 29
+    d, (idx, w) = oracle_tables(oracle, n, nsyn, seed)
+    sim = oracle.Sim(d, idx, w)
+    sim.run(60, threads=8)
+    with g4s.Network(n, nsyn, seed=seed) as net:
+        if p:
+            net.set_geometry(p)
+        gp, _ = net.geometry()
+        assert gp > 1 and (p == 0 or gp == p)
+        assert net.delivery() == want and (nsyn >= 24 * gp) == (want == 1)
+        net.run(60, 4)
+        assert np.array_equal(np.stack(net.raster()), np.stack(sim.raster()))
+        compare_state(net, sim)
+
+
 @pytest.mark.parametrize("n,drive,p,mode", [(100_000, 1.0, 0, 0), (50_000, 1.5, 8, 0), (50_000, 1.5, 8, 1),
                                             (300_000, 1.5, 0, 0), (3000, 1.0, 1, 0)])
 def test_block_threads_768_same_results(g4s, n, drive, p, mode):
     """The 768-thread team kernel gives the 1024-thread kernel's results bit for bit in every
-    delivery path: the flat mapping (N=100,000), segment runs and one lane per spike on
+    delivery path: the flat mapping (N=100,000), segment runs and eight-lane groups on
     6,250-neuron slices, the dense list of large steps (N=300,000 at drive 1.5), one CTA."""
     nsyn, out = 1000, []
     for threads in (1024, 768):
@@ -375,7 +396,7 @@ def test_team_without_interleaved_rows(g4s, p, delivery):
     """The team kernel's segment reads come from the interleaved (target, weight) rows; a
     network that finds no room for them (an allocation failure injected on the host) runs
     on the separate target and weight arrays with identical results.  8 CTAs: 6,250-neuron
-    slices, segment runs (0) or one lane per spike (1); the default geometry adds the flat
+    slices, segment runs (0) or eight lanes a spike (1); the default geometry adds the flat
     mapping."""
     from gpu4snn_gb300 import _lib
     n, nsyn, seed, steps = 50_000, 1000, 41, 300
