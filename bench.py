@@ -88,6 +88,15 @@ class ClockSampler:
                                          stdout=self.f, stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
             self.proc = None
+        # the timed region starts once the sampler has written its first sample, so that its
+        # start-up (loading the management library) stays out of it (once, on a fresh host, a
+        # lone timed launch that began with the sampler's start-up measured 30 times its
+        # usual time)
+        t0 = time.perf_counter()
+        while self.proc and self.proc.poll() is None and time.perf_counter() - t0 < 3.0:
+            if os.path.getsize(self.path) > 0:
+                break
+            time.sleep(0.02)
         return self
 
     def __exit__(self, *a):
