@@ -781,7 +781,7 @@ __device__ void team_run(const TeamItem &it, int rank, unsigned char *s_raw, Tea
         // step's spikes in batches of 32 as in the run mapping (`wpb` warps sharing a batch's
         // rounds when there are fewer batches than warps); a batch is walked in 8 rounds of 4
         // spikes, lane group g (lanes 8g .. 8g+7) reading spike 4r+g's segment in contiguous
-        // 32-synapse steps, four reads a lane in flight.  No search: a segment's synapses
+        // 64-synapse steps, eight reads a lane in flight.  No search: a segment's synapses
         // need no shuffles to find their spike.  The next batch's ids and bounds are loaded
         // while the current one is walked.
         const uint64_t pkeep = policy_evict_last();
@@ -810,18 +810,18 @@ __device__ void team_run(const TeamItem &it, int rank, unsigned char *s_raw, Tea
           for (int r = wi; r < 8; r += wpb) {
             const long long rb = __shfl_sync(0xFFFFFFFFu, rowb, r * 4 + grp);
             const int ln = __shfl_sync(0xFFFFFFFFu, len, r * 4 + grp);
-            for (int k0 = 0; k0 < ln; k0 += 32) {
-              int t[4];
-              float w[4];
+            for (int k0 = 0; k0 < ln; k0 += 64) {
+              int t[8];
+              float w[8];
 #pragma unroll
-              for (int u = 0; u < 4; ++u) {
+              for (int u = 0; u < 8; ++u) {
                 const int k = k0 + u * 8 + sub;
                 t[u] = -1;
                 w[u] = 0.0f;
                 if (k < ln) synapse(rb + k, t[u], w[u]);
               }
 #pragma unroll
-              for (int u = 0; u < 4; ++u)
+              for (int u = 0; u < 8; ++u)
                 if (t[u] >= 0) acc_add(base_a, base_b, (unsigned)(t[u] - (int)lo), wfix(w[u]));
             }
           }
