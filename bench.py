@@ -51,6 +51,8 @@ WORKLOADS = {
     "n25k": (25_000, 1000, 500, 1.0, 5),  # small profiling case: 0.2 GB of tables, still > L2
     "n300k": (300_000, 1000, 50, 1.0, 6),  # profiling case for large-N delivery: 2.4 GB of tables
     "n100k_200": (100_000, 1000, 200, 1.0, 2),  # profiling case: the N=100,000 network, 200-step launches
+    "n30k_s4k": (30_000, 4000, 100, 1.0, 7),  # profiling case for long segments (~26 synapses a rank, the
+                                              # eight-lane group delivery): 1.9 GB of tables with their copy
 }
 # algorithmic bytes: delivery = spikes x Nsyn x (4 B target + 4 B weight) and the spike
 # statistics (32 B read + 32 B written per spike); the neuron state (v,u read + write 16 B
