@@ -514,6 +514,8 @@ def main():
     ap.add_argument("--algorithm", default="AUTO")
     ap.add_argument("--block-threads", type=int, default=0,
                     help="threads per CTA of the SKL team kernel, 1024 or 768 (0: default / autotuned)")
+    ap.add_argument("--delivery", type=int, default=-1,
+                    help="delivery mapping of a multi-CTA SKL team: -1 automatic, 0 segment runs, 1 eight lanes a spike")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
     ap.add_argument("--raster-budget-mb", type=int, default=0, help="device raster buffer per chunk (0: default)")
@@ -546,6 +548,8 @@ def main():
     net = g.Network(n, nsyn, seed=seed, drive_scale=drive, record_raster=False, raster_budget_bytes=budget)
     if a.block_threads:
         net.set_block_threads(a.block_threads)
+    if a.delivery != -1:
+        net.set_geometry(0, a.delivery)
     schemes = None
     if not a.no_schemes:
         schemes = schemes_leg(g, net, nsyn, min(T, 2048))
