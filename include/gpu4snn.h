@@ -153,7 +153,9 @@ int g4s_net_get_delivery(g4s_net *net, int32_t *delivery);
 
 /* Autotuner (replaces the reference's occupancy-based launch configurator,
  * gpu4snn.cu:780-838, 959-1079): times the candidate schemes (SKL with teams of 1, 2, 4, ...
- * CTAs, AB, AP) on `probe_steps` steps of this network from a device snapshot of its state,
+ * CTAs at both CTA sizes, by segment runs and, where a team's segments average 12 synapses or
+ * more, by eight-lane groups; AB, AP) on `probe_steps` steps of this network from a device
+ * snapshot of its state,
  * restores the state (the simulation is unchanged), and keeps the fastest for ALG_AUTO on
  * this handle and, process-wide, for networks of the same size, fan-out and firing rate
  * (log2 buckets).  Outputs (any may be NULL): the scheme, its team size, us per step. */
