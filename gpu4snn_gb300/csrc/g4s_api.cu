@@ -882,6 +882,12 @@ static int absorb_chunk(g4s_net *n, int cs, int64_t *spikes) {
   return G4S_OK;
 }
 
+// Delivery mapping of a network's multi-CTA team: the one set or tuned, else eight-lane
+// groups when a rank's segment of a row holds kGroupMinSegment synapses or more on average.
+static int deliver_mode_of(const g4s_net *n) {
+  if (n->deliver_mode != kDeliverAuto) return n->deliver_mode;
+  return n->team_p > 1 && (int64_t)n->v.nsyn >= (int64_t)kGroupMinSegment * n->team_p ? kDeliverGroup : kDeliverRun;
+}
 
 // ---------------------------------------------------------------------------------------
 // One launch of the team kernel over several networks (a "round"): network i advances
@@ -892,13 +898,6 @@ static int absorb_chunk(g4s_net *n, int cs, int64_t *spikes) {
 // it and checks every network's status words.  Between the two, the host may work on the
 // previous round's results, but must not touch the pinned per-step buffers (the round's
 // graph writes them at its end) nor the networks' device arrays.
-// Delivery mapping of a network's multi-CTA team: the one set or tuned, else eight-lane
-// groups when a rank's segment of a row holds kGroupMinSegment synapses or more on average.
-static int deliver_mode_of(const g4s_net *n) {
-  if (n->deliver_mode != kDeliverAuto) return n->deliver_mode;
-  return n->team_p > 1 && (int64_t)n->v.nsyn >= (int64_t)kGroupMinSegment * n->team_p ? kDeliverGroup : kDeliverRun;
-}
-
 static int team_round_start(g4s_net *const *nets, const int *steps, const bool *last, int count, TeamLaunch &L,
                             cudaStream_t s, unsigned long long limit_ns, int stall) {
   std::vector<int> order;

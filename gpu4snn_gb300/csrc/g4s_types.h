@@ -86,7 +86,8 @@ constexpr int kDeliverAuto = -1;
 constexpr int kDeliverRun = 0;
 constexpr int kDeliverGroup = 1;
 // mean synapses of a rank's segment of a row (Nsyn / team) from which kDeliverAuto takes the
-// eight-lane groups (measured: ~20 synapses even, 53 and 66 a quarter faster than the runs)
+// eight-lane groups (measured in the team kernel: even with the runs at ~26 synapses, 14%
+// faster per step at ~66)
 constexpr int kGroupMinSegment = 24;
 
 }  // namespace g4s
