@@ -359,6 +359,26 @@ def test_weights_of_every_magnitude(g4s, oracle, p):
         compare_state(net, sim)
 
 
+def test_group_delivery_dense_list(g4s, oracle):
+    """The eight-lane group delivery on steps whose ids overflow the shared-memory window and
+    are read, tagged, from the dense global list: 8 CTAs of 16,384 neurons (a 1,728-id
+    window), segments of ~37 synapses (Nsyn 300 / 8, so the automatic choice is the groups),
+    a strong drive; against the oracle."""
+    n, nsyn, seed, drive, steps, p = 131_072, 300, 33, 2.0, 40, 8
+    d = oracle.make_desc(n, nsyn, seed, drive_scale=drive)
+    idx, w = oracle.conn_philox(d)
+    sim = oracle.Sim(d, idx, w)
+    sim.run(steps, threads=16)
+    with g4s.Network(n, nsyn, seed=seed, drive_scale=drive) as net:
+        net.set_geometry(p)
+        assert net.geometry() == (p, n // p) and net.delivery() == 1
+        net.run(steps, 4)
+        assert sim.counts().max() > 1728  # the dense-list path runs
+        assert np.array_equal(net.counts(), sim.counts())
+        assert np.array_equal(np.stack(net.raster()), np.stack(sim.raster()))
+        compare_state(net, sim)
+
+
 def test_large_steps_dense_list(g4s, oracle):
     """Steps with more than 4096 spikes (the ids go through the dense global list instead of
     the shared-memory window) and ranks with more than 31 spikes (ids beyond the record
