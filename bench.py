@@ -53,6 +53,8 @@ WORKLOADS = {
     "n100k_200": (100_000, 1000, 200, 1.0, 2),  # profiling case: the N=100,000 network, 200-step launches
     "n30k_s4k": (30_000, 4000, 100, 1.0, 7),  # profiling case for long segments (~26 synapses a rank, the
                                               # eight-lane group delivery): 1.9 GB of tables with their copy
+    "n25k_s10k": (25_000, 10_000, 50, 1.0, 8),  # profiling case with the segment length of N=250,000 x
+                                                # 10,000 (~66 synapses a rank): 4 GB of tables with their copy
 }
 # algorithmic bytes: delivery = spikes x Nsyn x (4 B target + 4 B weight) and the spike
 # statistics (32 B read + 32 B written per spike); the neuron state (v,u read + write 16 B
