@@ -419,7 +419,9 @@ def timed_leg(g, net, name, cfg, alg, a, pg, local, drive_override):
     upd_ms = sum(r[4] for r in runs)
     deliv_ms = max(1e-9, sum(r[5] for r in runs) - upd_ms)
     if last_alg == g.ALG_SKL and team > 0:
-        kname = f"k_team (SKL team kernel: {team} CTAs x {net.block_threads()} threads, {slice_} neurons per CTA)"
+        mapping = {0: ", segment runs", 1: ", eight-lane groups"}.get(net.delivery(), "")
+        kname = (f"k_team (SKL team kernel: {team} CTAs x {net.block_threads()} threads, {slice_} neurons per CTA"
+                 f"{mapping})")
     elif last_alg == g.ALG_SKL:
         kname = "k_persistent (SKL global-atomic kernel)"
     else:
@@ -561,6 +563,7 @@ def main():
         tuned = {"algorithm": talg, "name": ALG_LABEL[talg], "team": tteam, "us_per_step": tus}
         net.run(8, alg)  # (applies the choice, so that its CTA size can be read back)
         tuned["block_threads"] = net.block_threads()
+        tuned["delivery"] = {0: "segment runs", 1: "eight-lane groups"}.get(net.delivery(), "one CTA")
     r = timed_leg(g, net, a.workload, cfg, alg, a, pg, local, drive_override)
     t_max = reduce_max(pg, r["dev_ms"])
     ev_all = reduce_sum(pg, float(r["events"]))
